@@ -1,0 +1,112 @@
+"""Build libwenofd.so (CUDA kernels + C ABI) and the `wenofd` driver for sm_103a.
+
+    python fd-weno-eulerequation_gb300/build.py [--force] [--verbose-ptxas]
+
+Compiles every translation unit in parallel, skipping objects newer than
+their sources, into fd-weno-eulerequation_gb300/_build/.  The FP64 parity
+units are compiled with -fmad=false; host C++ with -ffp-contract=off so the
+initial conditions round like the reference's.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(PKG, "csrc")
+HOST = os.path.join(PKG, "host")
+OUT = os.path.join(PKG, "_build")
+ROOT = os.path.dirname(PKG)
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + os.path.join(CUDA_HOME, "include"),
+             "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+
+# translation unit -> extra flags
+CUDA_UNITS = {
+    "stage_fp64.cu": ["-fmad=false"],
+    "stage_fp32.cu": [],
+    "aux_kernels.cu": ["-fmad=false"],
+}
+CXX_UNITS = ["capi.cpp", "cases.cpp"]
+
+LIB = os.path.join(OUT, "libwenofd.so")
+EXE = os.path.join(OUT, "wenofd")
+
+
+def _deps() -> list[str]:
+    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) + \
+        [os.path.join(ROOT, "include", "wenofd.h"), os.path.abspath(__file__)]
+
+
+def _stale(obj: str, src: str) -> bool:
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(p) > t for p in [src] + _deps())
+
+
+def _run(cmd: list[str]) -> str:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> str:
+    os.makedirs(OUT, exist_ok=True)
+    jobs = []
+    objs = []
+    for unit, extra in CUDA_UNITS.items():
+        src = os.path.join(CSRC, unit)
+        obj = os.path.join(OUT, unit + ".o")
+        objs.append(obj)
+        if force or verbose_ptxas or _stale(obj, src):
+            cmd = [NVCC] + ARCH + NVCC_FLAGS + extra + ["-c", src, "-o", obj]
+            if verbose_ptxas:
+                cmd += ["-Xptxas", "-v"]
+            jobs.append(cmd)
+    cxx = shutil.which(os.environ.get("CXX", "g++")) or "g++"
+    for unit in CXX_UNITS:
+        src = os.path.join(CSRC, unit)
+        obj = os.path.join(OUT, unit + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src):
+            jobs.append([cxx] + CXX_FLAGS + ["-c", src, "-o", obj])
+    log = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for out in ex.map(_run, jobs):
+            log.append(out)
+    if jobs or not os.path.exists(LIB):
+        lib_dir = os.path.join(CUDA_HOME, "lib64")
+        _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-Xlinker", "-rpath," + lib_dir] + objs + ["-o", LIB])
+    probe = os.path.join(OUT, "pipe_peaks")
+    probe_src = os.path.join(CSRC, "pipe_peaks.cu")
+    if force or not os.path.exists(probe) or os.path.getmtime(probe_src) > os.path.getmtime(probe):
+        _run([NVCC] + ARCH + ["-O3", "-std=c++17", probe_src, "-o", probe])
+    host_srcs = [os.path.join(HOST, f) for f in ("WENOFD.cpp", "main.cpp")]
+    if all(os.path.exists(p) for p in host_srcs) and (force or not os.path.exists(EXE) or any(
+            os.path.getmtime(p) > os.path.getmtime(EXE) for p in host_srcs + [LIB, os.path.join(HOST, "WENOFD.hpp")])):
+        _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include"),
+              "-I" + HOST] + host_srcs + ["-L" + OUT, "-lwenofd", "-Wl,-rpath,$ORIGIN", "-o", EXE])
+    return "".join(log)
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--verbose-ptxas", action="store_true")
+    a = ap.parse_args()
+    out = build(a.force, a.verbose_ptxas)
+    if out.strip():
+        sys.stdout.write(out)
+    print(LIB)

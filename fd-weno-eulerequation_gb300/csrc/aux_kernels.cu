@@ -1,0 +1,345 @@
+// Boundary fill, time-step reduction, time-loop control and FP64 norm
+// kernels.  Compiled with -fmad=false like the FP64 stage: the time step is
+// part of the parity contract.
+#include "wenofd_internal.h"
+
+#include <math.h>
+
+namespace wenofd {
+
+namespace {
+
+constexpr int kReduceThreads = 256;
+constexpr int kReduceBlocks = 2 * 152;  // two CTAs per SM of a GB300
+
+__device__ __forceinline__ long long at(const Geom &g, int r, int ei, int ej) {
+  return r * g.plane + (long long)ei * g.pitch + ej;
+}
+
+// exchangeGhostCellsValue (src/WENOFD.cpp:850-929, one rank) + setBoundary
+// (998-1159).  Every ghost node a stencil reads -- x ghosts on interior
+// rows, y ghosts on interior columns -- is a function of interior nodes
+// only, so all of them are filled in one pass:
+//   x, periodic  : ghost[sx-k] = U[ex-1-k], ghost[ex-1+k] = U[sx+k]
+//                  (node-based: the duplicated end node is skipped)
+//   SYMMETRIC    : mirror about the boundary node, ghost[sx-k] = U[sx+k]
+//   SLIP         : mirror and negate the normal momentum
+//   SPECIAL      : initial-condition value at the boundary node (table)
+// The y direction uses the bottom condition on both sides (line 1009).
+// Corner ghosts (x ghost and y ghost at once) are never read by the sweeps
+// (lines 513-797) and are not written.
+__global__ void k_bc_fill(Geom g, double *U, const double *special, const int *active) {
+  if (active && *active == 0) return;
+  const int nxg = 4 * g.nx, nyg = 4 * g.ny;
+  const int total = 2 * nyg + 2 * nxg;
+  const int sx = kGhost, ex = kGhost + g.nx, sy = kGhost, ey = kGhost + g.ny;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    if (t < 2 * nyg) {  // x ghosts on interior rows
+      const int side = t / nyg, rem = t - side * nyg;
+      const int e1 = rem / g.ny + 1, ej = sy + (rem - (e1 - 1) * g.ny);
+      const int bc = side == 0 ? g.bc_left : g.bc_right;
+      const int dst = side == 0 ? sx - e1 : ex - 1 + e1;
+      int src;
+      if (bc == kPeriod) src = side == 0 ? ex - 1 - e1 : sx + e1;
+      else src = side == 0 ? sx + e1 : ex - 1 - e1;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double v;
+        if (bc == kSpecial) v = special[8 * g.nxt + (side * 4 + r) * g.nyt + ej];
+        else v = U[at(g, r, src, ej)];
+        if (bc == kSlip && r == 1) v *= -1;
+        U[at(g, r, dst, ej)] = v;
+      }
+    } else {  // y ghosts on interior columns
+      const int u = t - 2 * nyg;
+      const int side = u / nxg, rem = u - side * nxg;
+      const int e1 = rem / g.nx + 1, ei = sx + (rem - (e1 - 1) * g.nx);
+      const int bc = g.bc_y;
+      const int dst = side == 0 ? sy - e1 : ey - 1 + e1;
+      int src;
+      if (bc == kPeriod) src = side == 0 ? ey - 1 - e1 : sy + e1;
+      else src = side == 0 ? sy + e1 : ey - 1 - e1;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double v;
+        if (bc == kSpecial) v = special[(side * 4 + r) * g.nxt + ei];
+        else v = U[at(g, r, ei, src)];
+        if (bc == kSlip && r == 2) v *= -1;
+        U[at(g, r, ei, dst)] = v;
+      }
+    }
+  }
+}
+
+// calculateDeltaT (src/WENOFD.cpp:398-452).  Per node the reference forms
+// tmp = cfl / (lx/dx + ly/dy) with lx = |u*1 + v*0| + c, ly = |u*0 + v*1| + c
+// (getMaxEigenValue(U, 1, 0) and (U, 0, 1), utils/equations.hpp:137-147) and
+// keeps the minimum.  Correctly rounded division is monotone, so
+// min(cfl/s) == cfl/max(s): the reduction keeps max(s), as IEEE bits (all s
+// are >= 0, where bit order is value order), and k_dt_finalize divides once.
+// A NaN s sets a flag instead of entering the maximum.
+__global__ void k_dt_reduce(Geom g, const double *U, Ctrl *c) {
+  if (!c->active) return;
+  const long long n = (long long)g.nx * g.ny;
+  const double gamma = g.gamma;
+  double smax = 0.0;
+  int nan_seen = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+    const long long base = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const double rho = U[base], mu = U[g.plane + base], mv = U[2 * g.plane + base], E = U[3 * g.plane + base];
+    const double u = mu / rho, v = mv / rho;
+    const double p = (gamma - 1.0) * (E - 0.5 * rho * (u * u + v * v));
+    const double cs = sqrt(gamma * p / rho);
+    const double lx = fabs(u * 1.0 + v * 0.0) + cs;
+    const double ly = fabs(u * 0.0 + v * 1.0) + cs;
+    const double s = lx / g.dx + ly / g.dy;
+    if (s != s) nan_seen = 1;
+    else if (s > smax) smax = s;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double other = __shfl_xor_sync(0xffffffffu, smax, o);
+    smax = other > smax ? other : smax;
+    nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
+  }
+  __shared__ double wmax[32];
+  __shared__ int wnan[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    wmax[warp] = smax;
+    wnan[warp] = nan_seen;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    int nn = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      m = wmax[w] > m ? wmax[w] : m;
+      nn |= wnan[w];
+    }
+    atomicMax(&c->max_s_bits, (unsigned long long)__double_as_longlong(m));
+    if (nn) atomicOr(&c->nan_flag, 1);
+  }
+}
+
+// Open the gate for one host-driven operation (calc_dt, rk_step, step).
+__global__ void k_ctrl_open(Ctrl *c) {
+  c->active = 1;
+  c->max_s_bits = 0ull;
+  c->nan_flag = 0;
+  c->error = 0;
+}
+
+// Start of a graph-driven step: run while |now - t_end| > 1e-9 (the loop
+// condition of src/WENOFD.cpp:213), no error, and under the step cap.
+__global__ void k_step_begin(Ctrl *c) {
+  c->active = (!c->done && !c->error && c->steps < c->max_steps) ? 1 : 0;
+}
+
+// dt = min(1.0, cfl / max s), then clipped to t_end - now
+// (src/WENOFD.cpp:401, 426-435).  NaN -> error NAN_DT (the reference aborts,
+// lines 437-442).
+__global__ void k_dt_finalize(Ctrl *c) {
+  if (!c->active) return;
+  const double ms = __longlong_as_double((long long)c->max_s_bits);
+  c->max_s_bits = 0ull;
+  if (c->nan_flag) {
+    c->nan_flag = 0;
+    c->error = 3;  // WENOFD_NAN_DT
+    c->active = 0;
+    return;
+  }
+  const double cand = c->cfl / ms;
+  double timestep = 1.0;
+  if (!(cand > timestep)) timestep = cand;
+  if (c->t_end - c->now < timestep) timestep = c->t_end - c->now;
+  if (timestep != timestep) {
+    c->error = 3;
+    c->active = 0;
+    return;
+  }
+  c->dt = timestep;
+}
+
+// m_now += dt; count++ (src/WENOFD.cpp:238-239), then the loop condition.
+__global__ void k_step_end(Ctrl *c) {
+  if (!c->active) return;
+  c->now += c->dt;
+  c->steps += 1;
+  c->done = !(fabs(c->now - c->t_end) > 1e-9);
+}
+
+__global__ void k_set_dt(Ctrl *c, double dt) {
+  c->dt = dt;
+  c->active = 1;
+}
+
+__global__ void k_set_time(Ctrl *c, double now) {
+  c->now = now;
+  c->done = !(fabs(now - c->t_end) > 1e-9);
+  c->error = 0;
+}
+
+__global__ void k_advance_setup(Ctrl *c, long long max_steps) {
+  c->max_steps = max_steps < 0 ? 0x7fffffffffffffffLL : c->steps + max_steps;
+  c->done = !(fabs(c->now - c->t_end) > 1e-9);
+  c->max_s_bits = 0ull;
+  c->nan_flag = 0;
+}
+
+__global__ void k_copy_interior(Geom g, const double *src, double *dst, const int *active) {
+  if (active && *active == 0) return;
+  const long long n = 4LL * g.nx * g.ny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int r = int(t / ((long long)g.nx * g.ny));
+    const long long rem = t - r * ((long long)g.nx * g.ny);
+    const int i = int(rem / g.ny), j = int(rem - (rem / g.ny) * g.ny);
+    const long long idx = at(g, r, kGhost + i, kGhost + j);
+    dst[idx] = src[idx];
+  }
+}
+
+// FP64 reductions in a fixed order: each block reduces a fixed slice to
+// partials[blk*4 + q]; k_reduce_final combines the blocks in index order.
+// kind 0: {max err, sum err, sum err^2} of density against the smooth case's
+// exact solution 1 + 0.2 sin(pi (x + y - t)) (utils/equations.hpp:438-439);
+// kind 1: sums of the four conserved variables.
+__global__ void k_reduce_blocks(Geom g, const double *U, int kind, double t, double xl, double yl,
+                                double *partials) {
+  const long long n = (long long)g.nx * g.ny;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const double gx = (xl + 0 * g.dx) - g.dx * kGhost;  // ghost-origin coordinate (src/WENOFD.cpp:76-79)
+  const double gy = yl - g.dy * kGhost;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const int i = int(p / g.ny), j = int(p - (p / g.ny) * g.ny);
+    const long long base = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    if (kind == 0) {
+      const double x = gx + (kGhost + i) * g.dx, y = gy + (kGhost + j) * g.dy;
+      const double uref = 1 + 0.2 * sin(M_PI * (x + y - t));
+      const double err = fabs(uref - U[base]);
+      acc[0] = err > acc[0] ? err : acc[0];
+      acc[1] += err;
+      acc[2] += err * err;
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[r] += U[r * g.plane + base];
+    }
+  }
+  __shared__ double sh[4][kReduceThreads];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) sh[q][threadIdx.x] = acc[q];
+  __syncthreads();
+  for (int w = kReduceThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double o = sh[q][threadIdx.x + w];
+        if (kind == 0 && q == 0) sh[q][threadIdx.x] = o > sh[q][threadIdx.x] ? o : sh[q][threadIdx.x];
+        else sh[q][threadIdx.x] += o;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_reduce_final(Geom g, int kind, const double *partials, int nblk, double *out) {
+  if (threadIdx.x != 0) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = 0; b < nblk; ++b)
+    for (int q = 0; q < 4; ++q) {
+      const double o = partials[b * 4 + q];
+      if (kind == 0 && q == 0) acc[0] = o > acc[0] ? o : acc[0];
+      else acc[q] += o;
+    }
+  if (kind == 0) {  // src/WENOFD.cpp:1359-1360
+    out[0] = acc[0];
+    out[1] = acc[1] / g.nx / g.ny;
+    out[2] = sqrt(acc[2] / g.nx / g.ny);
+  } else {
+    for (int q = 0; q < 4; ++q) out[q] = acc[q];
+  }
+}
+
+int grid_for(long long work, int threads) {
+  long long b = (work + threads - 1) / threads;
+  if (b > 152LL * 16) b = 152LL * 16;
+  return int(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lambda, int bc_left,
+               int bc_right, int bc_y, int gravity) {
+  Geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nxt = nx + 2 * kGhost;
+  g.nyt = ny + 2 * kGhost;
+  g.pitch = (g.nyt + 31) / 32 * 32;
+  g.plane = (long long)g.nxt * g.pitch;
+  g.dx = dx;
+  g.dy = dy;
+  g.gamma = gamma;
+  g.zp_lambda = zp_lambda;
+  g.bc_left = bc_left;
+  g.bc_right = bc_right;
+  g.bc_y = bc_y;
+  g.gravity = gravity;
+  return g;
+}
+
+cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s) {
+  const long long work = 8LL * (g.nx + g.ny);
+  k_bc_fill<<<grid_for(work, 256), 256, 0, s>>>(g, U, special, active);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream_t s) {
+  k_dt_reduce<<<grid_for((long long)g.nx * g.ny, 256), 256, 0, s>>>(g, U, c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctrl_open(Ctrl *c, cudaStream_t s) {
+  k_ctrl_open<<<1, 1, 0, s>>>(c);
+  return cudaGetLastError();
+}
+cudaError_t launch_step_begin(Ctrl *c, cudaStream_t s) {
+  k_step_begin<<<1, 1, 0, s>>>(c);
+  return cudaGetLastError();
+}
+cudaError_t launch_dt_finalize(Ctrl *c, cudaStream_t s) {
+  k_dt_finalize<<<1, 1, 0, s>>>(c);
+  return cudaGetLastError();
+}
+cudaError_t launch_step_end(Ctrl *c, cudaStream_t s) {
+  k_step_end<<<1, 1, 0, s>>>(c);
+  return cudaGetLastError();
+}
+cudaError_t launch_set_dt(Ctrl *c, double dt, cudaStream_t s) {
+  k_set_dt<<<1, 1, 0, s>>>(c, dt);
+  return cudaGetLastError();
+}
+cudaError_t launch_set_time(Ctrl *c, double now, cudaStream_t s) {
+  k_set_time<<<1, 1, 0, s>>>(c, now);
+  return cudaGetLastError();
+}
+cudaError_t launch_advance_setup(Ctrl *c, long long max_steps, cudaStream_t s) {
+  k_advance_setup<<<1, 1, 0, s>>>(c, max_steps);
+  return cudaGetLastError();
+}
+cudaError_t launch_copy_interior(const Geom &g, const double *src, double *dst, const int *active, cudaStream_t s) {
+  k_copy_interior<<<grid_for(4LL * g.nx * g.ny, 256), 256, 0, s>>>(g, src, dst, active);
+  return cudaGetLastError();
+}
+
+int reduce_blocks() { return kReduceBlocks; }
+
+cudaError_t launch_reduce(const Geom &g, const double *U, int kind, double t, double xl, double yl,
+                          double *partials, double *out, cudaStream_t s) {
+  k_reduce_blocks<<<kReduceBlocks, kReduceThreads, 0, s>>>(g, U, kind, t, xl, yl, partials);
+  k_reduce_final<<<1, 32, 0, s>>>(g, kind, partials, kReduceBlocks, out);
+  return cudaGetLastError();
+}
+
+}  // namespace wenofd

@@ -1,0 +1,634 @@
+// Implementation of the C ABI declared in include/wenofd.h.
+//
+// One handle = one whole-domain solve resident on one GPU: three FP64
+// state arrays (U^n and two stage buffers; the reference's m_Uh / m_Un /
+// m_rhs, include/WENOFD.hpp:73-75), a SPECIAL boundary table, and a device
+// control block that carries dt, the time and the loop flags so the time
+// loop never waits on the host.
+#include "../../include/wenofd.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "cases.h"
+#include "wenofd_internal.h"
+
+using wenofd::Ctrl;
+using wenofd::Geom;
+using wenofd::StageArgs;
+
+struct wenofd_solver {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // created by the handle
+  int testcase = 0, nx = 0, ny = 0, rk = 2, scheme = 1, precision = 0, tile_i = 0;
+  double cfl = 0.5;
+  wenofd::CaseSpec cs;
+  Geom g{};
+  double *S = nullptr, *A = nullptr, *B = nullptr;  // U^n, stage buffers
+  size_t state_bytes = 0;
+  double *special = nullptr;
+  double *partials = nullptr, *red_out = nullptr;
+  Ctrl *ctrl = nullptr;
+  Ctrl *ctrl_host = nullptr;    // pinned mirror
+  double *red_host = nullptr;   // pinned, 4 doubles
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  long long graph_kernels = 0;  // kernel nodes in the graph
+  long long launches = 0;       // kernels enqueued so far (graph replays included)
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string &msg) {
+  g_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                     \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(WENOFD_CUDA_ERROR, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// trim of utils/readConfig.hpp:12-28: strip ' ' at both ends and one
+// trailing '\r'.
+std::string trim(const std::string &s) {
+  const size_t first = s.find_first_not_of(' ');
+  if (first == std::string::npos) return std::string();
+  size_t last = s.find_last_not_of(' ');
+  if (s[last] == '\r') {
+    if (last == first) return std::string();
+    --last;
+  }
+  return s.substr(first, last - first + 1);
+}
+
+// CConfig::read, utils/readConfig.hpp:39-80.
+int read_config(const char *path, std::map<std::string, std::string> &opt) {
+  std::ifstream in(path);
+  if (!in.is_open()) return fail(WENOFD_BAD_CONFIG, std::string("Failed to open file ") + path);
+  std::string line;
+  while (std::getline(in, line)) {
+    if (line.empty() || line[0] == '#' || line[0] == '\r') continue;
+    const size_t eq = line.find('=');
+    if (eq == std::string::npos) continue;  // the reference prints "Invalid line" and skips it
+    opt[trim(line.substr(0, eq))] = trim(line.substr(eq + 1));
+  }
+  return WENOFD_OK;
+}
+
+// std::stoi / std::stod semantics: leading number, rest ignored.
+bool get_int(const std::map<std::string, std::string> &o, const char *k, int &v, bool required) {
+  auto it = o.find(k);
+  if (it == o.end()) return !required;
+  try {
+    v = std::stoi(it->second);
+  } catch (...) {
+    return false;
+  }
+  return true;
+}
+
+bool get_double(const std::map<std::string, std::string> &o, const char *k, double &v, bool required) {
+  auto it = o.find(k);
+  if (it == o.end()) return !required;
+  try {
+    v = std::stod(it->second);
+  } catch (...) {
+    return false;
+  }
+  return true;
+}
+
+int check_handle(const wenofd_solver *s) {
+  if (!s) return fail(WENOFD_BAD_ARG, "null solver handle");
+  return WENOFD_OK;
+}
+
+int sync(wenofd_solver *s) {
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  return WENOFD_OK;
+}
+
+int launch_stage(wenofd_solver *s, const double *in, const double *un, double *out, double a, double b,
+                 double c, int mode) {
+  StageArgs args;
+  args.uin = in;
+  args.un = un;
+  args.uout = out;
+  args.a = a;
+  args.b = b;
+  args.c = c;
+  args.dt = &s->ctrl->dt;
+  args.active = &s->ctrl->active;
+  args.mode = mode;
+  CUDA_TRY(wenofd::launch_bc_fill(s->g, const_cast<double *>(in), s->special, &s->ctrl->active, s->stream));
+  s->launches += 2;
+  if (s->precision == WENOFD_FP32) {
+    CUDA_TRY(wenofd::launch_stage_fp32(s->g, args, s->scheme, s->tile_i, s->stream));
+  } else {
+    CUDA_TRY(wenofd::launch_stage_fp64(s->g, args, s->scheme, s->tile_i, s->stream));
+  }
+  return WENOFD_OK;
+}
+
+// RunRK1/2/3 (src/WENOFD.cpp:301-396), dt from the control block.  Stage k
+// reads its input with a halo and writes a different buffer; the last stage
+// writes U^{n+1} over U^n, which it reads only at the node itself.
+int enqueue_rk(wenofd_solver *s) {
+  int rc;
+  double *S = s->S, *A = s->A, *B = s->B;
+  switch (s->rk) {
+    case 0:  // U += dt * rhs, as (1*U + 0*U) + (1*dt)*rhs (same rounding)
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      CUDA_TRY(wenofd::launch_copy_interior(s->g, A, S, &s->ctrl->active, s->stream));
+      s->launches += 1;
+      return WENOFD_OK;
+    case 1:
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      return launch_stage(s, A, S, S, 0.5, 0.5, 0.5, wenofd::kModeRK);
+    case 2:
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      if ((rc = launch_stage(s, A, S, B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0, wenofd::kModeRK))) return rc;
+      return launch_stage(s, B, S, S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, wenofd::kModeRK);
+  }
+  return fail(WENOFD_BAD_CONFIG, "Error: Invalid Runge-Kutta method");
+}
+
+// One graph-driven step: gate, dt reduction, dt, stages, time update.
+int enqueue_step(wenofd_solver *s) {
+  CUDA_TRY(wenofd::launch_step_begin(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
+  int rc = enqueue_rk(s);
+  if (rc) return rc;
+  CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
+  s->launches += 4;
+  return WENOFD_OK;
+}
+
+int read_ctrl(wenofd_solver *s) {
+  CUDA_TRY(cudaMemcpyAsync(s->ctrl_host, s->ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+int copy_interior(wenofd_solver *s, double *dst_base, const double *src_base, size_t dst_pitch_b,
+                  size_t src_pitch_b, bool to_device, cudaMemcpyKind kind) {
+  const size_t plane_host = size_t(s->nx) * s->ny;
+  for (int r = 0; r < 4; ++r) {
+    const size_t dev_off = size_t(r) * s->g.plane + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost;
+    double *dst = to_device ? dst_base + dev_off : dst_base + r * plane_host;
+    const double *src = to_device ? src_base + r * plane_host : src_base + dev_off;
+    CUDA_TRY(cudaMemcpy2DAsync(dst, dst_pitch_b, src, src_pitch_b, size_t(s->ny) * sizeof(double), s->nx, kind,
+                               s->stream));
+  }
+  return WENOFD_OK;
+}
+
+int upload(wenofd_solver *s, const double *src, cudaMemcpyKind kind) {
+  return copy_interior(s, s->S, src, s->g.pitch * sizeof(double), s->ny * sizeof(double), true, kind);
+}
+
+int download(wenofd_solver *s, const double *dev_full, double *dst, cudaMemcpyKind kind) {
+  return copy_interior(s, dst, dev_full, s->ny * sizeof(double), s->g.pitch * sizeof(double), false, kind);
+}
+
+void release(wenofd_solver *s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  cudaFree(s->S);
+  cudaFree(s->A);
+  cudaFree(s->B);
+  cudaFree(s->special);
+  cudaFree(s->partials);
+  cudaFree(s->red_out);
+  cudaFree(s->ctrl);
+  cudaFreeHost(s->ctrl_host);
+  cudaFreeHost(s->red_host);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+}
+
+int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver **out) {
+  if (!out) return fail(WENOFD_BAD_ARG, "null output pointer");
+  *out = nullptr;
+  int testcase, nx, ny, rk, scheme, precision = 0, device = 0, tile_i = 0;
+  double cfl, t_end = -1.0;
+  long long seed_ll = 0;
+  // src/WENOFD.cpp:24-40
+  if (!get_int(opt, "TESTCASE", testcase, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing TESTCASE");
+  if (!get_int(opt, "RKMETH", rk, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing RKMETH");
+  if (!get_int(opt, "SCHEME", scheme, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing SCHEME");
+  if (!get_double(opt, "CFL", cfl, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing CFL");
+  if (!get_int(opt, "ELEMNUMX", nx, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing ELEMNUMX");
+  if (!get_int(opt, "ELEMNUMY", ny, true)) return fail(WENOFD_BAD_CONFIG, "bad or missing ELEMNUMY");
+  if (!get_int(opt, "PRECISION", precision, false)) return fail(WENOFD_BAD_CONFIG, "bad PRECISION");
+  if (!get_int(opt, "DEVICE", device, false)) return fail(WENOFD_BAD_CONFIG, "bad DEVICE");
+  if (!get_int(opt, "TILE_I", tile_i, false)) return fail(WENOFD_BAD_CONFIG, "bad TILE_I");
+  if (!get_double(opt, "TEND", t_end, false)) return fail(WENOFD_BAD_CONFIG, "bad TEND");
+  {
+    auto it = opt.find("SEED");
+    if (it != opt.end()) {
+      try {
+        seed_ll = std::stoll(it->second);
+      } catch (...) {
+        return fail(WENOFD_BAD_CONFIG, "bad SEED");
+      }
+    }
+  }
+  if (rk < 0 || rk > 2) return fail(WENOFD_BAD_CONFIG, "Error: Invalid Runge-Kutta method");
+  if (scheme < 0 || scheme > 3) return fail(WENOFD_BAD_CONFIG, "the scheme is not supported");
+  if (precision < 0 || precision > 1) return fail(WENOFD_BAD_CONFIG, "PRECISION must be 0 (FP64) or 1 (FP32)");
+  if (nx < 6 || ny < 6) return fail(WENOFD_BAD_CONFIG, "ELEMNUMX and ELEMNUMY must be at least 6");
+  if (nx > 65536 || ny > 65536) return fail(WENOFD_BAD_CONFIG, "ELEMNUMX and ELEMNUMY must be at most 65536");
+  if (!(cfl > 0.0)) return fail(WENOFD_BAD_CONFIG, "CFL must be positive");
+
+  wenofd::CaseSpec cs;
+  try {
+    cs = wenofd::make_case(testcase, (uint64_t)seed_ll);
+  } catch (const std::exception &e) {
+    return fail(WENOFD_BAD_CONFIG, e.what());
+  }
+  if (t_end > 0) cs.t_end = t_end;
+
+  wenofd_solver *s = new wenofd_solver();
+  s->device = device;
+  s->testcase = testcase;
+  s->nx = nx;
+  s->ny = ny;
+  s->rk = rk;
+  s->scheme = scheme;
+  s->precision = precision;
+  s->tile_i = tile_i;
+  s->cfl = cfl;
+  s->cs = cs;
+  const double dx = (cs.xr - cs.xl) / (nx - 1);  // src/WENOFD.cpp:73-74
+  const double dy = (cs.yr - cs.yl) / (ny - 1);
+  s->g = wenofd::make_geom(nx, ny, dx, dy, cs.gamma, std::pow(dx, 2.0 / 3.0), cs.bc_left, cs.bc_right,
+                           cs.bc_bottom, cs.gravity);
+
+  auto bail = [&](int rc) {
+    release(s);
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(device)) != cudaSuccess)
+    return bail(fail(WENOFD_CUDA_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+  if ((e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(fail(WENOFD_CUDA_ERROR, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+  s->stream = s->own_stream;
+  s->state_bytes = size_t(4) * s->g.plane * sizeof(double);
+  const std::vector<double> tab = wenofd::special_table(cs, nx, ny, dx, dy);
+  const int nblk = wenofd::reduce_blocks();
+  bool ok = cudaMalloc(&s->S, s->state_bytes) == cudaSuccess && cudaMalloc(&s->A, s->state_bytes) == cudaSuccess &&
+            cudaMalloc(&s->B, s->state_bytes) == cudaSuccess &&
+            cudaMalloc(&s->special, tab.size() * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&s->partials, size_t(nblk) * 4 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&s->red_out, 4 * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&s->ctrl, sizeof(Ctrl)) == cudaSuccess &&
+            cudaMallocHost(&s->ctrl_host, sizeof(Ctrl)) == cudaSuccess &&
+            cudaMallocHost(&s->red_host, 4 * sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    return bail(fail(WENOFD_CUDA_ERROR, "device allocation failed"));
+  }
+  ok = cudaMemsetAsync(s->S, 0, s->state_bytes, s->stream) == cudaSuccess &&
+       cudaMemsetAsync(s->A, 0, s->state_bytes, s->stream) == cudaSuccess &&
+       cudaMemsetAsync(s->B, 0, s->state_bytes, s->stream) == cudaSuccess &&
+       cudaMemcpyAsync(s->special, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream) ==
+           cudaSuccess;
+  Ctrl c0{};
+  c0.now = 0.0;
+  c0.t_end = cs.t_end;
+  c0.cfl = cfl;
+  c0.max_steps = 0x7fffffffffffffffLL;
+  c0.done = !(std::fabs(0.0 - cs.t_end) > 1e-9);
+  *s->ctrl_host = c0;
+  ok = ok && cudaMemcpyAsync(s->ctrl, s->ctrl_host, sizeof(Ctrl), cudaMemcpyHostToDevice, s->stream) == cudaSuccess &&
+       cudaStreamSynchronize(s->stream) == cudaSuccess;
+  if (!ok) return bail(fail(WENOFD_CUDA_ERROR, "device initialisation failed"));
+  *out = s;
+  return WENOFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wenofd_last_error(void) { return g_error.c_str(); }
+
+const char *wenofd_version(void) { return "wenofd-gb300 0.1 (sm_103a)"; }
+
+int wenofd_create(const char *const *keys, const char *const *values, int n, wenofd_solver **out) {
+  if (n < 0 || (n > 0 && (!keys || !values))) return fail(WENOFD_BAD_ARG, "bad key/value arrays");
+  std::map<std::string, std::string> opt;
+  for (int i = 0; i < n; ++i) {
+    if (!keys[i] || !values[i]) return fail(WENOFD_BAD_ARG, "null key or value");
+    opt[trim(keys[i])] = trim(values[i]);
+  }
+  return create_from_map(opt, out);
+}
+
+int wenofd_create_from_file(const char *config_path, wenofd_solver **out) {
+  if (!config_path) return fail(WENOFD_BAD_ARG, "null config path");
+  std::map<std::string, std::string> opt;
+  int rc = read_config(config_path, opt);
+  if (rc) return rc;
+  return create_from_map(opt, out);
+}
+
+int wenofd_destroy(wenofd_solver *s) {
+  if (!s) return WENOFD_OK;
+  release(s);
+  return WENOFD_OK;
+}
+
+int wenofd_set_stream(wenofd_solver *s, void *cuda_stream) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(cudaStreamSynchronize(s->stream));
+  s->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : s->own_stream;
+  return WENOFD_OK;
+}
+
+int wenofd_get_info(const wenofd_solver *s, wenofd_info *info) {
+  if (int rc = check_handle(s)) return rc;
+  if (!info) return fail(WENOFD_BAD_ARG, "null info");
+  wenofd_solver *m = const_cast<wenofd_solver *>(s);
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = read_ctrl(m)) return rc;
+  info->nx = s->nx;
+  info->ny = s->ny;
+  info->testcase = s->testcase;
+  info->scheme = s->scheme;
+  info->rk = s->rk;
+  info->precision = s->precision;
+  info->bc_left = s->cs.bc_left;
+  info->bc_right = s->cs.bc_right;
+  info->bc_bottom = s->cs.bc_bottom;
+  info->bc_top = s->cs.bc_top;
+  info->has_exact = s->cs.exact;
+  info->pitch = s->g.pitch;
+  info->dx = s->g.dx;
+  info->dy = s->g.dy;
+  info->cfl = s->cfl;
+  info->t_end = s->cs.t_end;
+  info->now = s->ctrl_host->now;
+  info->gamma = s->cs.gamma;
+  info->xl = s->cs.xl;
+  info->xr = s->cs.xr;
+  info->yl = s->cs.yl;
+  info->yr = s->cs.yr;
+  info->steps = s->ctrl_host->steps;
+  info->launches = s->launches;
+  info->graph_steps = s->graph_steps;
+  return WENOFD_OK;
+}
+
+int wenofd_initialize(wenofd_solver *s) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  std::vector<double> host(size_t(4) * s->nx * s->ny);
+  wenofd::initial_state(s->cs, s->nx, s->ny, s->g.dx, s->g.dy, host.data());
+  if (int rc = upload(s, host.data(), cudaMemcpyHostToDevice)) return rc;
+  CUDA_TRY(wenofd::launch_set_time(s->ctrl, 0.0, s->stream));
+  if (int rc = sync(s)) return rc;
+  if (int rc = read_ctrl(s)) return rc;
+  s->ctrl_host->steps = 0;
+  CUDA_TRY(cudaMemcpyAsync(s->ctrl, s->ctrl_host, sizeof(Ctrl), cudaMemcpyHostToDevice, s->stream));
+  return sync(s);
+}
+
+int wenofd_set_state(wenofd_solver *s, const double *host_state) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_state) return fail(WENOFD_BAD_ARG, "null state");
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = upload(s, host_state, cudaMemcpyHostToDevice)) return rc;
+  return sync(s);
+}
+
+int wenofd_get_state(wenofd_solver *s, double *host_state) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_state) return fail(WENOFD_BAD_ARG, "null state");
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = download(s, s->S, host_state, cudaMemcpyDeviceToHost)) return rc;
+  return sync(s);
+}
+
+int wenofd_set_state_device(wenofd_solver *s, const double *dev_state) {
+  if (int rc = check_handle(s)) return rc;
+  if (!dev_state) return fail(WENOFD_BAD_ARG, "null state");
+  CUDA_TRY(cudaSetDevice(s->device));
+  return upload(s, dev_state, cudaMemcpyDeviceToDevice);
+}
+
+int wenofd_get_state_device(wenofd_solver *s, double *dev_state) {
+  if (int rc = check_handle(s)) return rc;
+  if (!dev_state) return fail(WENOFD_BAD_ARG, "null state");
+  CUDA_TRY(cudaSetDevice(s->device));
+  return download(s, s->S, dev_state, cudaMemcpyDeviceToDevice);
+}
+
+int wenofd_get_state_ghosted(wenofd_solver *s, double *host_full) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_full) return fail(WENOFD_BAD_ARG, "null state");
+  CUDA_TRY(cudaSetDevice(s->device));
+  const size_t hp = size_t(s->g.nxt) * s->g.nyt;
+  for (int r = 0; r < 4; ++r)
+    CUDA_TRY(cudaMemcpy2DAsync(host_full + r * hp, s->g.nyt * sizeof(double), s->S + r * s->g.plane,
+                               s->g.pitch * sizeof(double), s->g.nyt * sizeof(double), s->g.nxt,
+                               cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+int wenofd_set_time(wenofd_solver *s, double now) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_set_time(s->ctrl, now, s->stream));
+  return sync(s);
+}
+
+int wenofd_fill_boundary(wenofd_solver *s) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
+  return sync(s);
+}
+
+int wenofd_get_flux(wenofd_solver *s, double *host_rhs) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
+  if (int rc = launch_stage(s, s->S, s->S, s->A, 0.0, 0.0, 0.0, wenofd::kModeRHS)) return rc;
+  if (host_rhs)
+    if (int rc = download(s, s->A, host_rhs, cudaMemcpyDeviceToHost)) return rc;
+  return sync(s);
+}
+
+int wenofd_calc_dt(wenofd_solver *s, double *dt) {
+  if (int rc = check_handle(s)) return rc;
+  if (!dt) return fail(WENOFD_BAD_ARG, "null dt");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
+  s->launches += 3;
+  if (int rc = read_ctrl(s)) return rc;
+  if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
+  *dt = s->ctrl_host->dt;
+  return WENOFD_OK;
+}
+
+int wenofd_rk_step(wenofd_solver *s, double dt) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_set_dt(s->ctrl, dt, s->stream));
+  if (int rc = enqueue_rk(s)) return rc;
+  return sync(s);
+}
+
+int wenofd_step(wenofd_solver *s, double *dt_out) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
+  if (int rc = enqueue_rk(s)) return rc;
+  CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
+  s->launches += 4;
+  if (int rc = read_ctrl(s)) return rc;
+  if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
+  if (dt_out) *dt_out = s->ctrl_host->dt;
+  return WENOFD_OK;
+}
+
+int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = read_ctrl(s)) return rc;
+  const long long start = s->ctrl_host->steps;
+  if (!s->graph) {
+    // One gated-off pass outside capture configures the kernels' shared
+    // memory limits on this device: the gate is closed (max_steps = steps),
+    // so every kernel returns at once.
+    CUDA_TRY(wenofd::launch_advance_setup(s->ctrl, 0, s->stream));
+    if (int rc = enqueue_step(s)) return rc;
+    if (int rc = sync(s)) return rc;
+    // Steps per graph launch: enough that launch latency is amortised on
+    // small grids, one step on large ones.
+    const long long cells = (long long)s->nx * s->ny;
+    s->graph_steps = int(std::max(1LL, std::min(64LL, (4LL << 20) / std::max(1LL, cells))));
+    cudaStream_t cap = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaStream_t keep = s->stream;
+    s->stream = cap;
+    cudaGraph_t graph = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int rc = WENOFD_OK;
+    const long long before = s->launches;
+    for (int k = 0; k < s->graph_steps && rc == WENOFD_OK; ++k) rc = enqueue_step(s);
+    s->graph_kernels = s->launches - before;
+    s->launches = before;
+    cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+    s->stream = keep;
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    CUDA_TRY(ce);
+    ce = cudaGraphInstantiate(&s->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    CUDA_TRY(ce);
+  }
+  CUDA_TRY(wenofd::launch_advance_setup(s->ctrl, max_steps, s->stream));
+  s->launches += 1;
+  for (;;) {
+    CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += s->graph_kernels;
+    if (int rc = read_ctrl(s)) return rc;
+    const Ctrl &c = *s->ctrl_host;
+    if (c.error) {
+      if (steps_done) *steps_done = c.steps - start;
+      return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
+    }
+    if (c.done || c.steps >= c.max_steps) break;
+  }
+  if (steps_done) *steps_done = s->ctrl_host->steps - start;
+  return WENOFD_OK;
+}
+
+int wenofd_error_norms(wenofd_solver *s, double out[3]) {
+  if (int rc = check_handle(s)) return rc;
+  if (!out) return fail(WENOFD_BAD_ARG, "null output");
+  if (!s->cs.exact) return fail(WENOFD_NO_EXACT, "this case has no exact solution");
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = read_ctrl(s)) return rc;
+  CUDA_TRY(wenofd::launch_reduce(s->g, s->S, 0, s->ctrl_host->now, s->cs.xl, s->cs.yl, s->partials, s->red_out,
+                                 s->stream));
+  CUDA_TRY(cudaMemcpyAsync(s->red_host, s->red_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (int rc = sync(s)) return rc;
+  std::memcpy(out, s->red_host, 3 * sizeof(double));
+  return WENOFD_OK;
+}
+
+int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
+  if (int rc = check_handle(s)) return rc;
+  if (!ms_per_launch || reps < 1) return fail(WENOFD_BAD_ARG, "bad arguments");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
+  s->launches += 1;
+  struct St { const double *in, *un; double *out; double a, b, c; };
+  std::vector<St> st;
+  if (s->rk == 2)
+    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}, {s->A, s->S, s->B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0},
+          {s->B, s->S, s->S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
+  else if (s->rk == 1)
+    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}, {s->A, s->S, s->S, 0.5, 0.5, 0.5}};
+  else
+    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}};
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  CUDA_TRY(cudaEventRecord(e0, s->stream));
+  for (int r = 0; r < reps; ++r)
+    for (const St &x : st) {
+      StageArgs a{x.in, x.un, x.out, x.a, x.b, x.c, &s->ctrl->dt, &s->ctrl->active, wenofd::kModeRK};
+      cudaError_t e = s->precision == WENOFD_FP32 ? wenofd::launch_stage_fp32(s->g, a, s->scheme, s->tile_i, s->stream)
+                                                  : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
+      CUDA_TRY(e);
+      s->launches += 1;
+    }
+  CUDA_TRY(cudaEventRecord(e1, s->stream));
+  CUDA_TRY(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms_per_launch = double(ms) / (double(reps) * st.size());
+  return WENOFD_OK;
+}
+
+int wenofd_conservation_sums(wenofd_solver *s, double out[4]) {
+  if (int rc = check_handle(s)) return rc;
+  if (!out) return fail(WENOFD_BAD_ARG, "null output");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_reduce(s->g, s->S, 1, 0.0, 0.0, 0.0, s->partials, s->red_out, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(s->red_host, s->red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (int rc = sync(s)) return rc;
+  std::memcpy(out, s->red_host, 4 * sizeof(double));
+  return WENOFD_OK;
+}
+
+}  // extern "C"

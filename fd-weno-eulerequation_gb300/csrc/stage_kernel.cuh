@@ -1,0 +1,205 @@
+// One RK stage of the WENO-FD hot path as a single fused tile kernel:
+// halo load, x sweep (flux split, characteristic WENO faces), y sweep, flux
+// differences, source term and the RK combination, with nothing but the
+// state in global memory.
+//
+// Replaces, per stage: assembleRHS (src/WENOFD.cpp:454-465) with
+// assembleBoundaryTerm's x sweep (513-649) and y sweep (652-797),
+// assembleSourceTerm (800-821), and the stage update of RunRK1/2/3
+// (301-396).  The boundary fill runs before it (k_bc_fill).
+//
+// Tile: TI nodes in x by TJ = 32 nodes in y (y is the contiguous axis, so a
+// warp spans one tile row).  The block stages the state of the tile plus a
+// 3-node halo in shared memory, computes the split fluxes of every node the
+// tile's faces need once, then the (TI+1) x TJ x-faces and TI x (TJ+1)
+// y-faces, and keeps the per-node x term in registers between the sweeps.
+// Shared-memory regions for the split fluxes and face fluxes are reused by
+// the y sweep.
+#pragma once
+
+#include "physics.cuh"
+
+namespace wenofd {
+namespace dev {
+
+template <typename T, int TI, int TJ>
+struct StageSmem {
+  static constexpr int HI = TI + 6, HJ = TJ + 6;
+  static constexpr int kU = 4 * HI * HJ;                                    // state + halo
+  static constexpr int kSplit = 4 * (HI * TJ > TI * HJ ? HI * TJ : TI * HJ);  // one of F+, F-
+  static constexpr int kFace = 4 * ((TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1));
+  static constexpr size_t bytes = sizeof(T) * (size_t(kU) + 2 * kSplit + kFace);
+};
+
+template <typename T, int SCHEME, int TI, int TJ, int NT>
+__global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
+  if (*a.active == 0) return;
+  using S = StageSmem<T, TI, TJ>;
+  constexpr int HI = S::HI, HJ = S::HJ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *Us = reinterpret_cast<T *>(smem_raw);
+  T *Fp = Us + S::kU;
+  T *Fm = Fp + S::kSplit;
+  T *Hf = Fm + S::kSplit;
+
+  const int i0 = blockIdx.y * TI;  // first interior node of the tile (0-based)
+  const int j0 = blockIdx.x * TJ;
+  const T gamma = T(g.gamma);
+  const T zpl = T(g.zp_lambda);
+
+  // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj
+  for (int t = threadIdx.x; t < 4 * HI * HJ; t += NT) {
+    const int r = t / (HI * HJ);
+    const int rem = t - r * (HI * HJ);
+    const int hi = rem / HJ, hj = rem - hi * HJ;
+    const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
+    T val = T(0);
+    if (ei < g.nxt && ej < g.nyt) val = T(a.uin[r * g.plane + (long long)ei * g.pitch + ej]);
+    Us[t] = val;
+  }
+  __syncthreads();
+
+  // --- x sweep: split fluxes of halo rows 0..HI-1, columns 3..3+TJ
+  for (int t = threadIdx.x; t < HI * TJ; t += NT) {
+    const int hi = t / TJ, j = t - hi * TJ;
+    T q[4], fm[4], fp[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) q[r] = Us[(r * HI + hi) * HJ + j + 3];
+    flux_split<T, 0>(gamma, q, fm, fp);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      Fp[(r * HI + hi) * TJ + j] = fp[r];
+      Fm[(r * HI + hi) * TJ + j] = fm[r];
+    }
+  }
+  __syncthreads();
+  // x faces f = 0..TI: face between tile nodes f-1 and f (halo rows f+2, f+3)
+  for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
+    const int f = t / TJ, j = t - f * TJ;
+    if (i0 + f > g.nx || j0 + j >= g.ny) continue;
+    T um[4], u0[4], out[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
+      u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
+    }
+    face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
+  }
+  __syncthreads();
+
+  // rhs = 0 + x term  (rhs zeroed in assembleRHS, then += in the x sweep)
+  constexpr int PPT = (TI * TJ + NT - 1) / NT;
+  T rhs[PPT][4];
+  const T dx = T(g.dx), dy = T(g.dy);
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int t = threadIdx.x + k * NT;
+    const int i = t / TJ, j = t - (t / TJ) * TJ;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      if (t < TI * TJ) {
+        const T hr = Hf[(r * (TI + 1) + i + 1) * TJ + j], hl = Hf[(r * (TI + 1) + i) * TJ + j];
+        rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
+      }
+    }
+  }
+  __syncthreads();
+
+  // --- y sweep: split fluxes of tile rows, halo columns 0..HJ-1
+  for (int t = threadIdx.x; t < TI * HJ; t += NT) {
+    const int i = t / HJ, hj = t - i * HJ;
+    T q[4], fm[4], fp[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) q[r] = Us[(r * HI + i + 3) * HJ + hj];
+    flux_split<T, 1>(gamma, q, fm, fp);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      Fp[(r * TI + i) * HJ + hj] = fp[r];
+      Fm[(r * TI + i) * HJ + hj] = fm[r];
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
+    const int i = t / (TJ + 1), f = t - i * (TJ + 1);
+    if (i0 + i >= g.nx || j0 + f > g.ny) continue;
+    T um[4], u0[4], out[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
+      u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
+    }
+    face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
+  }
+  __syncthreads();
+
+  // --- y term, source, RK combination, store
+  const double dt = *a.dt;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int t = threadIdx.x + k * NT;
+    if (t >= TI * TJ) continue;
+    const int i = t / TJ, j = t - i * TJ;
+    if (i0 + i >= g.nx || j0 + j >= g.ny) continue;
+    T rr[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const T hr = Hf[(r * TI + i) * (TJ + 1) + j + 1], hl = Hf[(r * TI + i) * (TJ + 1) + j];
+      rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
+    }
+    const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+    if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
+      const T g_g0 = T(1.0);
+      rr[3] += Us[(2 * HI + i + 3) * HJ + j + 3] * g_g0;
+      rr[2] += Us[(0 * HI + i + 3) * HJ + j + 3] * g_g0;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const long long idx = r * g.plane + gidx;
+      if (a.mode == kModeRHS) {
+        a.uout[idx] = double(rr[r]);
+      } else {
+        const double un = a.un[idx], ui = a.uin[idx];
+        a.uout[idx] = a.a * un + a.b * ui + a.c * dt * double(rr[r]);
+      }
+    }
+  }
+}
+
+// Host-side launcher for one precision: picks the kernel instance for the
+// scheme and tile height, sets its shared-memory size, launches it.
+template <typename T, int TI, int NT>
+cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cudaStream_t s) {
+  constexpr int TJ = 32;
+  using Sm = StageSmem<T, TI, TJ>;
+  const dim3 grid((g.ny + TJ - 1) / TJ, (g.nx + TI - 1) / TI);
+  void (*fn)(Geom, StageArgs) = nullptr;
+  switch (scheme) {
+    case kWenoJS: fn = k_stage<T, kWenoJS, TI, TJ, NT>; break;
+    case kWenoZ: fn = k_stage<T, kWenoZ, TI, TJ, NT>; break;
+    case kWenoZP: fn = k_stage<T, kWenoZP, TI, TJ, NT>; break;
+    case kWenoZPI: fn = k_stage<T, kWenoZPI, TI, TJ, NT>; break;
+    default: return cudaErrorInvalidValue;
+  }
+  // The dynamic shared-memory limit is a per-device function attribute: set
+  // it on the first launch per device (before any stream capture; the C ABI
+  // runs one plain step before it captures a graph).
+  static unsigned long long configured[4] = {0, 0, 0, 0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured[scheme & 3] & bit)) {
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Sm::bytes));
+    if (e != cudaSuccess) return e;
+    configured[scheme & 3] |= bit;
+  }
+  fn<<<grid, NT, Sm::bytes, s>>>(g, a);
+  return cudaGetLastError();
+}
+
+}  // namespace dev
+}  // namespace wenofd

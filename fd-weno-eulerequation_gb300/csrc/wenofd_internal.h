@@ -1,0 +1,85 @@
+// Internal declarations shared by the CUDA translation units and the C-ABI
+// implementation.  Not installed; the public boundary is include/wenofd.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace wenofd {
+
+constexpr int kGhost = 4;  // ghost nodes per side (src/WENOFD.cpp:36)
+
+// BOUNDARYTYPE (utils/equations.hpp:45-51)
+enum Boundary { kPeriod = 0, kSlip = 1, kSpecial = 2, kSymmetric = 3 };
+// SCHEMETYPE (utils/equations.hpp:15-21)
+enum Scheme { kWenoJS = 0, kWenoZ = 1, kWenoZP = 2, kWenoZPI = 3 };
+
+// Device layout of one state array: [4][nxt][pitch] float64, element
+// (r, ei, ej) at r*plane + ei*pitch + ej, ej (y) fastest, the reference's
+// m_Uh[ei][ej].vector[r] in structure-of-arrays form.  Interior nodes are
+// ei in [4, 4+nx), ej in [4, 4+ny).  pitch >= ny+8 is a multiple of 32
+// elements so every row starts on a 256-byte boundary.
+struct Geom {
+  int nx, ny;     // interior nodes (ELEMNUMX, ELEMNUMY)
+  int nxt, nyt;   // nx + 8, ny + 8
+  int pitch;      // row pitch in elements
+  long long plane;
+  double dx, dy, gamma;
+  double zp_lambda;  // pow(dx, 2/3), WENO-ZP (include/Utility.hpp:531; dx also in y, src/WENOFD.cpp:836)
+  int bc_left, bc_right, bc_y;  // y uses the bottom condition on both sides (src/WENOFD.cpp:1009)
+  int gravity;                  // RTI source term (src/WENOFD.cpp:800-821)
+};
+
+// Device-resident control block of the time loop.  All fields are written
+// by single-thread control kernels or by the host between launches.
+struct Ctrl {
+  double now, t_end, cfl, dt;
+  unsigned long long max_s_bits;  // max over nodes of lx/dx + ly/dy, as IEEE bits (all >= 0)
+  long long steps, max_steps;
+  int active;    // this step runs (set per step)
+  int done;      // |now - t_end| <= 1e-9 (src/WENOFD.cpp:213)
+  int nan_flag;  // a NaN wave speed was seen by the reduction
+  int error;     // sticky wenofd_status of the device loop
+};
+
+// Arguments of one RK stage launch.  uin is read with a 3-node halo (its
+// ghosts must be filled); un is read only at the node itself and may alias
+// uout (the last stage writes U^{n+1} over U^n in place).
+struct StageArgs {
+  const double *uin;
+  const double *un;
+  double *uout;
+  double a, b, c;      // uout = a*un + b*uin + c*dt*rhs  (src/WENOFD.cpp:391-394)
+  const double *dt;    // device pointer (Ctrl::dt)
+  const int *active;   // device pointer (Ctrl::active); 0 -> return
+  int mode;            // kModeRK or kModeRHS (uout = rhs)
+};
+enum { kModeRK = 0, kModeRHS = 1 };
+
+Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lambda, int bc_left,
+               int bc_right, int bc_y, int gravity);
+
+// stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form)
+cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
+cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
+
+// aux_kernels.cu
+cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s);
+cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream_t s);
+cudaError_t launch_ctrl_open(Ctrl *c, cudaStream_t s);
+cudaError_t launch_step_begin(Ctrl *c, cudaStream_t s);
+cudaError_t launch_dt_finalize(Ctrl *c, cudaStream_t s);
+cudaError_t launch_step_end(Ctrl *c, cudaStream_t s);
+cudaError_t launch_set_dt(Ctrl *c, double dt, cudaStream_t s);
+cudaError_t launch_set_time(Ctrl *c, double now, cudaStream_t s);
+cudaError_t launch_advance_setup(Ctrl *c, long long max_steps, cudaStream_t s);
+cudaError_t launch_copy_interior(const Geom &g, const double *src, double *dst, const int *active, cudaStream_t s);
+// FP64 reductions over interior nodes into partials[nblk*4] then out[4]
+// (deterministic order).  kind 0: {Linf, L1, L2} of density against the
+// smooth case's exact solution at time t (xl, yl: domain origin);
+// kind 1: sums of the 4 conserved variables.
+int reduce_blocks();
+cudaError_t launch_reduce(const Geom &g, const double *U, int kind, double t, double xl, double yl,
+                          double *partials, double *out, cudaStream_t s);
+
+}  // namespace wenofd

@@ -1,0 +1,226 @@
+"""ctypes binding of the wenofd C ABI (include/wenofd.h).
+
+The solver runs only through libwenofd.so's CUDA kernels: there is no CPU
+fallback, and importing this module raises if the library is missing.
+
+    import wenofd
+    s = wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": 800, "ELEMNUMY": 800,
+                       "RKMETH": 2, "CFL": 0.7, "SCHEME": 1, "SEED": 7})
+    s.initialize()
+    s.advance(max_steps=100)
+    U = s.get_state()          # float64 (4, NX, NY), ej fastest
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+LIB_PATH = os.path.join(PKG, "_build", "libwenofd.so")
+
+OK, BAD_CONFIG, CUDA_ERROR, NAN_DT, TIMEOUT, BAD_ARG, NO_EXACT = range(7)
+FP64, FP32 = 0, 1
+SMOOTH, RIEMANN1, RIEMANN2, RTI, RIEMANN_SEEDED, SHEAR = range(6)
+WENOJS, WENOZ, WENOZP, WENOZPI = range(4)
+RK1, RK2, RK3 = range(3)
+
+
+class WenofdError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"wenofd status {status}: {message}")
+        self.status = status
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int),
+        ("testcase", C.c_int), ("scheme", C.c_int), ("rk", C.c_int), ("precision", C.c_int),
+        ("bc_left", C.c_int), ("bc_right", C.c_int), ("bc_bottom", C.c_int), ("bc_top", C.c_int),
+        ("has_exact", C.c_int), ("pitch", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("cfl", C.c_double), ("t_end", C.c_double),
+        ("now", C.c_double), ("gamma", C.c_double),
+        ("xl", C.c_double), ("xr", C.c_double), ("yl", C.c_double), ("yr", C.c_double),
+        ("steps", C.c_longlong),
+        ("launches", C.c_longlong),
+        ("graph_steps", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libwenofd.so (build it with fd-weno-eulerequation_gb300/build.py)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libwenofd.so not built: {LIB_PATH} (run fd-weno-eulerequation_gb300/build.py)")
+        L = C.CDLL(LIB_PATH)
+        H = C.c_void_p
+        P = C.POINTER(C.c_double)
+        L.wenofd_last_error.restype = C.c_char_p
+        L.wenofd_version.restype = C.c_char_p
+        L.wenofd_create.argtypes = [C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.c_int, C.POINTER(H)]
+        L.wenofd_create_from_file.argtypes = [C.c_char_p, C.POINTER(H)]
+        L.wenofd_destroy.argtypes = [H]
+        L.wenofd_set_stream.argtypes = [H, C.c_void_p]
+        L.wenofd_get_info.argtypes = [H, C.POINTER(Info)]
+        for name in ("wenofd_initialize", "wenofd_fill_boundary"):
+            getattr(L, name).argtypes = [H]
+        for name in ("wenofd_set_state", "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux",
+                     "wenofd_calc_dt", "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums"):
+            getattr(L, name).argtypes = [H, P]
+        L.wenofd_set_state_device.argtypes = [H, C.c_void_p]
+        L.wenofd_get_state_device.argtypes = [H, C.c_void_p]
+        L.wenofd_set_time.argtypes = [H, C.c_double]
+        L.wenofd_rk_step.argtypes = [H, C.c_double]
+        L.wenofd_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
+        L.wenofd_time_stages.argtypes = [H, C.c_int, P]
+        for f in ("wenofd_create", "wenofd_create_from_file", "wenofd_destroy", "wenofd_set_stream",
+                  "wenofd_get_info", "wenofd_initialize", "wenofd_fill_boundary", "wenofd_set_state",
+                  "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux", "wenofd_calc_dt",
+                  "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_set_state_device",
+                  "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
+                  "wenofd_time_stages"):
+            getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != OK:
+        raise WenofdError(rc, lib().wenofd_last_error().decode())
+
+
+def _dptr(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Solver:
+    """One device-resident solve behind the C ABI (the CWENOFD hot path)."""
+
+    def __init__(self, config: dict | None = None, config_file: str | None = None):
+        L = lib()
+        self._h = C.c_void_p()
+        if config_file is not None:
+            _check(L.wenofd_create_from_file(config_file.encode(), C.byref(self._h)))
+        else:
+            keys = [str(k).encode() for k in config]
+            vals = [(repr(v) if isinstance(v, float) else str(v)).encode() for v in config.values()]
+            K = (C.c_char_p * len(keys))(*keys)
+            V = (C.c_char_p * len(vals))(*vals)
+            _check(L.wenofd_create(K, V, len(keys), C.byref(self._h)))
+        i = self.info()
+        self.nx, self.ny = i.nx, i.ny
+
+    def close(self) -> None:
+        if self._h:
+            lib().wenofd_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def info(self) -> Info:
+        i = Info()
+        _check(lib().wenofd_get_info(self._h, C.byref(i)))
+        return i
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check(lib().wenofd_set_stream(self._h, C.c_void_p(stream_ptr or 0)))
+
+    def initialize(self) -> None:
+        _check(lib().wenofd_initialize(self._h))
+
+    def set_state(self, U: np.ndarray) -> None:
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        if U.shape != (4, self.nx, self.ny):
+            raise ValueError(f"state shape {U.shape} != {(4, self.nx, self.ny)}")
+        _check(lib().wenofd_set_state(self._h, _dptr(U)))
+
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty((4, self.nx, self.ny)) if out is None else out
+        _check(lib().wenofd_get_state(self._h, _dptr(out)))
+        return out
+
+    def get_state_ghosted(self) -> np.ndarray:
+        out = np.empty((4, self.nx + 8, self.ny + 8))
+        _check(lib().wenofd_get_state_ghosted(self._h, _dptr(out)))
+        return out
+
+    def set_time(self, now: float) -> None:
+        _check(lib().wenofd_set_time(self._h, now))
+
+    def fill_boundary(self) -> None:
+        _check(lib().wenofd_fill_boundary(self._h))
+
+    def get_flux(self) -> np.ndarray:
+        out = np.empty((4, self.nx, self.ny))
+        _check(lib().wenofd_get_flux(self._h, _dptr(out)))
+        return out
+
+    def calc_dt(self) -> float:
+        dt = np.zeros(1)
+        _check(lib().wenofd_calc_dt(self._h, _dptr(dt)))
+        return float(dt[0])
+
+    def rk_step(self, dt: float) -> None:
+        _check(lib().wenofd_rk_step(self._h, dt))
+
+    def step(self) -> float:
+        dt = np.zeros(1)
+        _check(lib().wenofd_step(self._h, _dptr(dt)))
+        return float(dt[0])
+
+    def advance(self, max_steps: int = -1) -> int:
+        n = C.c_longlong(0)
+        _check(lib().wenofd_advance(self._h, max_steps, C.byref(n)))
+        return n.value
+
+    def error_norms(self) -> np.ndarray:
+        out = np.zeros(3)
+        _check(lib().wenofd_error_norms(self._h, _dptr(out)))
+        return out
+
+    def set_state_ptr(self, host_ptr: int) -> None:
+        """Upload from a raw host address (e.g. pinned memory), [4][NX][NY] float64."""
+        _check(lib().wenofd_set_state(self._h, C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double))))
+
+    def get_state_ptr(self, host_ptr: int) -> None:
+        _check(lib().wenofd_get_state(self._h, C.cast(C.c_void_p(host_ptr), C.POINTER(C.c_double))))
+
+    def time_stages(self, reps: int) -> float:
+        ms = np.zeros(1)
+        _check(lib().wenofd_time_stages(self._h, reps, _dptr(ms)))
+        return float(ms[0])
+
+    def conservation_sums(self) -> np.ndarray:
+        out = np.zeros(4)
+        _check(lib().wenofd_conservation_sums(self._h, _dptr(out)))
+        return out
+
+
+EXPORTED = [
+    "wenofd_last_error", "wenofd_version", "wenofd_create", "wenofd_create_from_file", "wenofd_destroy",
+    "wenofd_set_stream", "wenofd_get_info", "wenofd_initialize", "wenofd_set_state", "wenofd_get_state",
+    "wenofd_set_state_device", "wenofd_get_state_device", "wenofd_get_state_ghosted", "wenofd_set_time",
+    "wenofd_fill_boundary", "wenofd_get_flux", "wenofd_calc_dt", "wenofd_rk_step", "wenofd_step",
+    "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
+]

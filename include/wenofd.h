@@ -1,0 +1,139 @@
+/*
+ * wenofd.h — C ABI of the GB300-native WENO finite-difference Euler solver.
+ *
+ * The entry points replace the per-step hot path of the reference solver
+ * class CWENOFD (infinity-07/FD-WENO-EulerEquation, include/WENOFD.hpp:28-124,
+ * src/WENOFD.cpp).  Each declaration names the reference member it stands
+ * in for.  One solver handle owns one whole-domain, device-resident state on
+ * one GPU; the reference's 1-D MPI slab decomposition and halo exchange
+ * (src/WENOFD.cpp:47-70, 850-929) become an in-place device ghost fill.
+ *
+ * Conventions
+ *  - Every function returns an int status (enum wenofd_status).  On failure
+ *    wenofd_last_error() returns a message for the calling thread.  Where the
+ *    reference aborts (MPI_Abort, exit) or throws, these return a status.
+ *  - Host-side state arrays are float64, interior nodes only, structure of
+ *    arrays [4][ELEMNUMX][ELEMNUMY] with ej (y) fastest: element (r, ei, ej)
+ *    is m_Uh[ei+4][ej+4].vector[r] of the reference.  r = rho, rho*u, rho*v, E.
+ *  - A handle is used by one host thread at a time.  Its work runs on one
+ *    CUDA stream (its own, or the caller's via wenofd_set_stream).
+ *  - No torch or other framework types cross this boundary.
+ */
+#ifndef WENOFD_H
+#define WENOFD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct wenofd_solver wenofd_solver;
+
+enum wenofd_status {
+  WENOFD_OK = 0,
+  WENOFD_BAD_CONFIG = 1, /* bad or missing config key (reference: std::stoi throws, invalid_argument) */
+  WENOFD_CUDA_ERROR = 2, /* a CUDA call failed */
+  WENOFD_NAN_DT = 3,     /* time step is NaN (reference: src/WENOFD.cpp:437-442 aborts) */
+  WENOFD_TIMEOUT = 4,    /* a bounded device-side wait gave up */
+  WENOFD_BAD_ARG = 5,    /* null pointer, size or mode out of range */
+  WENOFD_NO_EXACT = 6    /* error norms asked for a case without an exact solution */
+};
+
+/* Arithmetic of the flux / reconstruction kernels.  FP64 reproduces the
+ * reference bit for bit.  FP32 keeps state, RK sums, the time-step reduction
+ * and all norms in FP64 and evaluates fluxes and reconstruction in FP32. */
+enum wenofd_precision { WENOFD_FP64 = 0, WENOFD_FP32 = 1 };
+
+/* Test cases: TESTCASETYPE (utils/equations.hpp:30-36) plus two seeded ones. */
+enum wenofd_testcase {
+  WENOFD_SMOOTH = 0, WENOFD_RIEMANN1 = 1, WENOFD_RIEMANN2 = 2, WENOFD_RTI = 3,
+  WENOFD_RIEMANN_SEEDED = 4, /* four-quadrant Riemann problem, quadrant states from SEED */
+  WENOFD_SHEAR = 5           /* periodic shear layer on [0,1]^2 with seeded noise */
+};
+
+typedef struct wenofd_info {
+  int nx, ny;             /* ELEMNUMX, ELEMNUMY (nodes incl. both boundary nodes) */
+  int testcase, scheme, rk, precision;
+  int bc_left, bc_right, bc_bottom, bc_top; /* BOUNDARYTYPE values */
+  int has_exact;          /* equation->u_exact_exist */
+  int pitch;              /* device row pitch, in elements */
+  double dx, dy, cfl, t_end, now, gamma;
+  double xl, xr, yl, yr;
+  long long steps;        /* completed time steps */
+  long long launches;     /* kernels this handle has enqueued (graph nodes counted per replay) */
+  int graph_steps;        /* time steps per CUDA-graph replay in wenofd_advance (0: not built yet) */
+} wenofd_info;
+
+/* Message describing the last failure on the calling thread ("" if none). */
+const char *wenofd_last_error(void);
+const char *wenofd_version(void);
+
+/* CConfig::read + CWENOFD::initializeSolver (utils/readConfig.hpp:39-80,
+ * src/WENOFD.cpp:10-164).  keys/values are the config.cfg pairs; required:
+ * TESTCASE, ELEMNUMX, ELEMNUMY, RKMETH, CFL, SCHEME (src/WENOFD.cpp:24-40).
+ * Optional keys the reference does not have: PRECISION (0 FP64, 1 FP32),
+ * SEED (seeded cases), TEND (overrides equation->outputtime), DEVICE,
+ * TILE_I (stage-kernel tile height; 0 = default). */
+int wenofd_create(const char *const *keys, const char *const *values, int n, wenofd_solver **out);
+/* Same, reading a config.cfg file with the reference's parser semantics
+ * (`key = value` lines, `#` comments, trimmed spaces and '\r'). */
+int wenofd_create_from_file(const char *config_path, wenofd_solver **out);
+int wenofd_destroy(wenofd_solver *s);
+/* Run this handle's work on the caller's cudaStream_t (NULL: back to the
+ * handle's own stream). */
+int wenofd_set_stream(wenofd_solver *s, void *cuda_stream);
+int wenofd_get_info(const wenofd_solver *s, wenofd_info *info);
+
+/* CWENOFD::initializeAve (src/WENOFD.cpp:165-188): initial condition of the
+ * configured case at every interior node; time and step count reset to 0. */
+int wenofd_initialize(wenofd_solver *s);
+/* Upload / download the interior state (host pointers, [4][NX][NY]). */
+int wenofd_set_state(wenofd_solver *s, const double *host_state);
+int wenofd_get_state(wenofd_solver *s, double *host_state);
+/* Same with device pointers (no host round trip; stream-ordered). */
+int wenofd_set_state_device(wenofd_solver *s, const double *dev_state);
+int wenofd_get_state_device(wenofd_solver *s, double *dev_state);
+/* Full state including the 4 ghost layers, [4][NX+8][NY+8] (host). */
+int wenofd_get_state_ghosted(wenofd_solver *s, double *host_full);
+int wenofd_set_time(wenofd_solver *s, double now);
+
+/* exchangeGhostCellsValue + setBoundary (src/WENOFD.cpp:850-929, 998-1159)
+ * on the current state, in place. */
+int wenofd_fill_boundary(wenofd_solver *s);
+/* CWENOFD::assembleRHS (src/WENOFD.cpp:454-465; assembleBoundaryTerm
+ * 481-798 is the "getFlux" of the reference README) of the current state:
+ * boundary fill, x and y characteristic WENO sweeps, source term.  The
+ * interior RHS [4][NX][NY] is written to host_rhs (may be NULL: kept on the
+ * device only). */
+int wenofd_get_flux(wenofd_solver *s, double *host_rhs);
+/* CWENOFD::calculateDeltaT (src/WENOFD.cpp:398-452) of the current state. */
+int wenofd_calc_dt(wenofd_solver *s, double *dt);
+/* CWENOFD::RunRK1/2/3 (src/WENOFD.cpp:301-396) with the given step, per
+ * RKMETH.  Does not advance the time. */
+int wenofd_rk_step(wenofd_solver *s, double dt);
+/* One iteration of the CWENOFD::run loop (src/WENOFD.cpp:213-239):
+ * calculateDeltaT, RunRK, m_now += dt.  dt_out may be NULL. */
+int wenofd_step(wenofd_solver *s, double *dt_out);
+/* The CWENOFD::run time loop (src/WENOFD.cpp:213-284) until |now - t_end|
+ * <= 1e-9 or max_steps more steps (max_steps < 0: no cap).  The time step
+ * never leaves the device; steps run in CUDA-graph chunks.  steps_done may
+ * be NULL. */
+int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done);
+/* CWENOFD::outputAccuracy norms (src/WENOFD.cpp:1308-1382) of density
+ * against the exact solution at the current time: out = {Linf, L1, L2},
+ * L1/L2 normalised by NX*NY.  FP64 device reduction. */
+int wenofd_error_norms(wenofd_solver *s, double out[3]);
+/* Interior sums of rho, rho*u, rho*v, E (FP64 device reduction). */
+int wenofd_conservation_sums(wenofd_solver *s, double out[4]);
+
+/* Measurement aid, no reference counterpart: replays the RK stage kernels of
+ * one step (RKMETH's stages, boundary fills excluded, dt as last set) `reps`
+ * times on the handle's stream between two CUDA events and returns the mean
+ * duration of one stage-kernel launch in milliseconds.  It advances the
+ * state; callers re-upload a state afterwards. */
+int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
