@@ -181,6 +181,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-headline", action="store_true",
+                    help="time the headline form only (no FP64 leg, error, e2e or CPU leg): for profiling")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -222,6 +224,13 @@ def main() -> None:
         s32, ms32, launches = time_form(wenofd, torch, wenofd.FP32, local, args.steps, args.warmup, stream)
     ms32 = max_over_ranks(ms32)
     value = world * args.steps * cells / (ms32 / 1e3)
+    if args.only_headline:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "steps": args.steps,
+                              "ms_per_step": ms32 / args.steps, "gpu_launches": launches,
+                              "note": "headline form only (profiling run)"}))
+        s32.close()
+        return
 
     # ---- plain FP64 WENO-Z (bitwise the reference) on the same GPU
     k64 = args.fp64_steps if args.fp64_steps is not None else max(2, min(args.steps, 5))

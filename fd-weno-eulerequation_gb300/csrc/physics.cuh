@@ -107,16 +107,14 @@ __device__ __forceinline__ T weno_js(T a, T b, T c, T d, T e) {
   return combine(w0, w1, w2, a, b, c, d, e);
 }
 
-// Ratio cap of the FP32 WENO-Z weights.  In FP64 tau/(beta+1e-20) squared
-// stays finite; in FP32 it overflows where a stencil is exactly flat
-// (beta = 0) next to a jump, so the FP32 form caps the ratio at 1e18 (its
-// square 1e36 is finite), which leaves the normalised weights unchanged to
-// FP32 precision.  The FP64 path applies no cap.
-template <typename T> __device__ __forceinline__ T zcap(T x) { return x; }
-template <> __device__ __forceinline__ float zcap<float>(float x) { return fminf(x, 1.0e18f); }
-
-// WENO-Z, include/Utility.hpp:457-504 (eps = 1e-20), the weight products
-// taken left to right: tau*inv*tau*inv.
+// WENO-Z, include/Utility.hpp:457-504 (eps = 1e-20).
+//
+// FP64: the weight products are taken left to right, tau*inv*tau*inv, as in
+// the reference (lines 489-491), with no guard.  FP32: (tau/(beta+1e-20))^2
+// overflows where a stencil is exactly flat (beta = 0) next to a jump, so the
+// ratio r is capped at 1e18 before squaring (r^2 <= 1e36 stays finite); a
+// weight that large already makes its stencil's normalised weight 1 to FP32
+// precision, so the cap changes nothing else.
 template <typename T>
 __device__ __forceinline__ void wenoz_weights(T a, T b, T c, T d, T e, T &w0, T &w1, T &w2) {
   T bm, b0, bp;
@@ -126,10 +124,16 @@ __device__ __forceinline__ void wenoz_weights(T a, T b, T c, T d, T e, T &w0, T 
   const T ib0 = tdiv(T(1.0), (b0 + eps));
   const T ibp = tdiv(T(1.0), (bp + eps));
   const T tau = tabs(bm - bp);
-  const T rm = zcap(tau * ibm), r0 = zcap(tau * ib0), rp = zcap(tau * ibp);
-  w0 = T(0.1) * (T(1.0) + (rm * tau * ibm));
-  w1 = T(0.6) * (T(1.0) + (r0 * tau * ib0));
-  w2 = T(0.3) * (T(1.0) + (rp * tau * ibp));
+  if constexpr (sizeof(T) == 4) {
+    const T rm = fminf(tau * ibm, 1.0e18f), r0 = fminf(tau * ib0, 1.0e18f), rp = fminf(tau * ibp, 1.0e18f);
+    w0 = T(0.1) * (T(1.0) + rm * rm);
+    w1 = T(0.6) * (T(1.0) + r0 * r0);
+    w2 = T(0.3) * (T(1.0) + rp * rp);
+  } else {
+    w0 = T(0.1) * (T(1.0) + (tau * ibm * tau * ibm));
+    w1 = T(0.6) * (T(1.0) + (tau * ib0 * tau * ib0));
+    w2 = T(0.3) * (T(1.0) + (tau * ibp * tau * ibp));
+  }
   const T ws = w0 + w1 + w2;
   w0 = tdiv(w0, ws);
   w1 = tdiv(w1, ws);
@@ -144,8 +148,16 @@ __device__ __forceinline__ T weno_z(T a, T b, T c, T d, T e) {
 }
 
 // pow(x, 2) of the reference's ZP/ZPI weights is evaluated as x*x, the
-// correctly rounded square, which is what glibc's pow returns for exponent 2.
+// correctly rounded square.  glibc's pow(x, 2) differs from it by one ulp on
+// about 0.1% of inputs, so WENO-ZP/ZPI agree with the reference to rounding
+// rather than bit for bit (WENO-JS and WENO-Z have no pow).
 template <typename T> __device__ __forceinline__ T sq(T x) { return x * x; }
+
+// FP32 ZP/ZPI: eps = 1e-40 is subnormal in FP32 and the weight ratios can
+// exceed the FP32 range, so the FP32 form divides with IEEE '/' (subnormal
+// safe) and caps each ratio term at 1e18 before it is squared or summed.
+template <typename T> __device__ __forceinline__ T zdiv(T a, T b) { return tdiv(a, b); }
+template <> __device__ __forceinline__ float zdiv<float>(float a, float b) { return fminf(a / b, 1.0e18f); }
 
 // WENO-ZP, include/Utility.hpp:505-558 (eps = 1e-40; lambda = pow(dx, 2/3)).
 template <typename T>
@@ -154,9 +166,9 @@ __device__ __forceinline__ T weno_zp(T a, T b, T c, T d, T e, T lambda) {
   betas(a, b, c, d, e, bm, b0, bp);
   const T tau = tabs(bm - bp);
   const T eps = T(1.0e-40);
-  T w0 = T(0.1) * (T(1) + sq(tdiv((tau + eps), (bm + eps))) + tdiv(lambda * (bm + eps), (tau + eps)));
-  T w1 = T(0.6) * (T(1) + sq(tdiv((tau + eps), (b0 + eps))) + tdiv(lambda * (b0 + eps), (tau + eps)));
-  T w2 = T(0.3) * (T(1) + sq(tdiv((tau + eps), (bp + eps))) + tdiv(lambda * (bp + eps), (tau + eps)));
+  T w0 = T(0.1) * (T(1) + sq(zdiv((tau + eps), (bm + eps))) + zdiv(lambda * (bm + eps), (tau + eps)));
+  T w1 = T(0.6) * (T(1) + sq(zdiv((tau + eps), (b0 + eps))) + zdiv(lambda * (b0 + eps), (tau + eps)));
+  T w2 = T(0.3) * (T(1) + sq(zdiv((tau + eps), (bp + eps))) + zdiv(lambda * (bp + eps), (tau + eps)));
   const T sum = w0 + w1 + w2;
   w0 = tdiv(w0, sum);
   w1 = tdiv(w1, sum);
@@ -175,11 +187,11 @@ __device__ __forceinline__ T weno_zpi(T a, T b, T c, T d, T e) {
   const T bmax = (bm < mx_in) ? mx_in : bm;
   const T mn_in = (bp < b0) ? bp : b0;  // std::min(beta, betap)
   const T bmin = (mn_in < bm) ? mn_in : bm;
-  const T alpha = T(1) - tdiv(bmin, (bmax + T(1e-40)));
+  const T alpha = T(1) - zdiv(bmin, (bmax + T(1e-40)));
   const T eps = T(1.0e-40);
-  T w0 = T(0.1) * (T(1) + sq(tdiv(tau, (bm + eps))) + tdiv(lambda * alpha * (bm), (bmax + eps)));
-  T w1 = T(0.6) * (T(1) + sq(tdiv(tau, (b0 + eps))) + tdiv(lambda * alpha * (b0), (bmax + eps)));
-  T w2 = T(0.3) * (T(1) + sq(tdiv(tau, (bp + eps))) + tdiv(lambda * alpha * (bp), (bmax + eps)));
+  T w0 = T(0.1) * (T(1) + sq(zdiv(tau, (bm + eps))) + zdiv(lambda * alpha * (bm), (bmax + eps)));
+  T w1 = T(0.6) * (T(1) + sq(zdiv(tau, (b0 + eps))) + zdiv(lambda * alpha * (b0), (bmax + eps)));
+  T w2 = T(0.3) * (T(1) + sq(zdiv(tau, (bp + eps))) + zdiv(lambda * alpha * (bp), (bmax + eps)));
   const T sum = w0 + w1 + w2;
   w0 = tdiv(w0, sum);
   w1 = tdiv(w1, sum);

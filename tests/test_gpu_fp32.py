@@ -1,0 +1,70 @@
+"""The FP32 precision form: flux and reconstruction arithmetic in FP32, state,
+RK sums and the time step in FP64.  Its results are compared with the FP64
+path (bitwise the reference) on the same inputs; the bounds below are the
+accepted error of the form and are written into the test."""
+import numpy as np
+import pytest
+
+import oracle as orc
+import wenofd
+from conftest import fixture_id, fixture_paths, load_fixture
+
+pytestmark = pytest.mark.gpu
+
+RHS_REL_TOL = 2e-4      # max |rhs32 - rhs64| / max |rhs64|
+STATE_REL_TOL = 1e-5    # max |U32 - U64| / max |U64| after the fixture's steps
+
+
+def _config(meta, precision):
+    cfg = {"TESTCASE": meta["testcase"], "ELEMNUMX": meta["nx"], "ELEMNUMY": meta["ny"],
+           "RKMETH": meta["rk"], "CFL": meta["cfl"], "SCHEME": meta["scheme"], "SEED": meta["seed"],
+           "PRECISION": precision}
+    if meta.get("t_end") is not None:
+        cfg["TEND"] = meta["t_end"]
+    return cfg
+
+
+@pytest.mark.parametrize("path", fixture_paths("rhs_"), ids=fixture_id)
+def test_fp32_rhs_close_to_reference(path):
+    fx = load_fixture(path)
+    m = fx["meta"]
+    with wenofd.Solver(_config(m, wenofd.FP32)) as s:
+        s.set_state(fx["init"])
+        rhs = s.get_flux()
+    assert np.all(np.isfinite(rhs))
+    err = np.max(np.abs(rhs - fx["rhs"])) / np.max(np.abs(fx["rhs"]))
+    assert err <= RHS_REL_TOL, err
+
+
+@pytest.mark.parametrize("path", fixture_paths("run_"), ids=fixture_id)
+def test_fp32_steps_close_to_reference(path):
+    fx = load_fixture(path)
+    m = fx["meta"]
+    with wenofd.Solver(_config(m, wenofd.FP32)) as s:
+        s.set_state(fx["init"])
+        n = s.advance(max_steps=m["steps"] if m["t_end"] is None else -1)
+        U = s.get_state()
+    assert n == m["steps"]
+    assert np.all(np.isfinite(U))
+    err = np.max(np.abs(U - fx["state"])) / np.max(np.abs(fx["state"]))
+    assert err <= STATE_REL_TOL, err
+
+
+@pytest.mark.parametrize("scheme", [orc.WENOJS, orc.WENOZ, orc.WENOZP, orc.WENOZPI])
+def test_fp32_shear_layer_stays_finite_and_close(scheme):
+    """The shear layer has flat stencils next to jumps (beta = 0 beside a
+    large tau), the case that overflows unguarded FP32 weights."""
+    n, steps = 256, 40
+    p = orc.Problem(orc.SHEAR, n, n, scheme, 2, 0.7, seed=5)
+    init = p.interior()
+    out = {}
+    for prec in (wenofd.FP64, wenofd.FP32):
+        with wenofd.Solver({"TESTCASE": 5, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7,
+                            "SCHEME": scheme, "SEED": 5, "PRECISION": prec}) as s:
+            s.set_state(init)
+            assert s.advance(max_steps=steps) == steps
+            out[prec] = s.get_state()
+    assert np.all(np.isfinite(out[wenofd.FP32]))
+    rho32, rho64 = out[wenofd.FP32][0], out[wenofd.FP64][0]
+    assert np.mean(np.abs(rho32 - rho64)) <= 1e-5
+    assert np.max(np.abs(rho32 - rho64)) <= 1e-3
