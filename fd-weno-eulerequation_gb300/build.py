@@ -36,6 +36,7 @@ CUDA_UNITS = {
     "stage_fp64.cu": ["-fmad=false"],
     "stage_fp32.cu": [],
     "aux_kernels.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
 }
 CXX_UNITS = ["capi.cpp", "cases.cpp"]
 

@@ -327,6 +327,12 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
 
 }  // namespace
 
+namespace wenofd {
+// Lets other translation units of the library report through
+// wenofd_last_error().
+void set_last_error(const std::string &msg) { g_error = msg; }
+}  // namespace wenofd
+
 extern "C" {
 
 const char *wenofd_last_error(void) { return g_error.c_str(); }

@@ -78,12 +78,15 @@ def lib() -> C.CDLL:
         L.wenofd_rk_step.argtypes = [H, C.c_double]
         L.wenofd_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
         L.wenofd_time_stages.argtypes = [H, C.c_int, P]
+        D = C.c_double
+        L.wenofd_calc_dt_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, D, D, D, D, D, D, C.c_void_p,
+                                             C.c_void_p]
         for f in ("wenofd_create", "wenofd_create_from_file", "wenofd_destroy", "wenofd_set_stream",
                   "wenofd_get_info", "wenofd_initialize", "wenofd_fill_boundary", "wenofd_set_state",
                   "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux", "wenofd_calc_dt",
                   "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_set_state_device",
                   "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
-                  "wenofd_time_stages"):
+                  "wenofd_time_stages", "wenofd_calc_dt_noalloc"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -223,4 +226,5 @@ EXPORTED = [
     "wenofd_set_state_device", "wenofd_get_state_device", "wenofd_get_state_ghosted", "wenofd_set_time",
     "wenofd_fill_boundary", "wenofd_get_flux", "wenofd_calc_dt", "wenofd_rk_step", "wenofd_step",
     "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
+    "wenofd_calc_dt_noalloc",
 ]

@@ -132,6 +132,26 @@ int wenofd_conservation_sums(wenofd_solver *s, double out[4]);
  * state; callers re-upload a state afterwards. */
 int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch);
 
+/* No counterpart in the reference.  calculateDeltaT (src/WENOFD.cpp:398-452
+ * arithmetic, bit for bit) of a caller-owned device state, for callers that
+ * must not allocate: an application whose GPU memory belongs to its own pool
+ * and that lends this library only its state buffers, or a time loop that
+ * cannot absorb cudaMalloc/cudaFree, which synchronise the whole device.
+ * Needs no handle and allocates nothing; it only enqueues two kernels.
+ *   dev_state  interior state, device memory, float64 [4][nx][ny] (ej fastest)
+ *   dev_dt     device double that receives dt, or NaN if a node's wave speed
+ *              is NaN (where the reference aborts)
+ *   stream     cudaStream_t (NULL: the default stream); the call returns
+ *              without waiting for the result.
+ * Limit: nx*ny <= 2^28 nodes (16384 x 16384); larger grids are rejected with
+ * WENOFD_BAD_ARG and a message.  Scratch: a fixed 8 KiB __device__ array in
+ * the library (per-block maxima), held by every GPU that loads the library
+ * until exit.  The first call on a device looks up that array's address
+ * (with the device current), so make it before any stream capture on that
+ * device.  All calls share the array: calls that overlap on the GPU race. */
+int wenofd_calc_dt_noalloc(const double *dev_state, int nx, int ny, double dx, double dy, double gamma,
+                           double cfl, double now, double t_end, double *dev_dt, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
