@@ -264,6 +264,25 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
     return fail(WENOFD_BAD_CONFIG, e.what());
   }
   if (t_end > 0) cs.t_end = t_end;
+  // Overrides of the EulerEquation parameters (utils/equations.hpp:58-70):
+  // a caller that sets xL..yR, euler_gamma or the boundary types on its
+  // equation object passes them here.
+  int bcs[4] = {cs.bc_left, cs.bc_right, cs.bc_bottom, cs.bc_top};
+  const char *bc_keys[4] = {"BC_LEFT", "BC_RIGHT", "BC_BOTTOM", "BC_TOP"};
+  for (int k = 0; k < 4; ++k) {
+    if (!get_int(opt, bc_keys[k], bcs[k], false) || bcs[k] < 0 || bcs[k] > 3)
+      return fail(WENOFD_BAD_CONFIG, std::string("bad ") + bc_keys[k]);
+  }
+  cs.bc_left = bcs[0];
+  cs.bc_right = bcs[1];
+  cs.bc_bottom = bcs[2];
+  cs.bc_top = bcs[3];
+  if (!get_double(opt, "XL", cs.xl, false) || !get_double(opt, "XR", cs.xr, false) ||
+      !get_double(opt, "YL", cs.yl, false) || !get_double(opt, "YR", cs.yr, false) ||
+      !get_double(opt, "GAMMA", cs.gamma, false) || !get_int(opt, "GRAVITY", cs.gravity, false))
+    return fail(WENOFD_BAD_CONFIG, "bad domain, GAMMA or GRAVITY value");
+  if (!(cs.xr > cs.xl) || !(cs.yr > cs.yl) || !(cs.gamma > 1.0))
+    return fail(WENOFD_BAD_CONFIG, "domain must have XR > XL, YR > YL and GAMMA > 1");
 
   wenofd_solver *s = new wenofd_solver();
   s->device = device;
@@ -465,6 +484,15 @@ int wenofd_set_time(wenofd_solver *s, double now) {
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_set_time(s->ctrl, now, s->stream));
+  return sync(s);
+}
+
+int wenofd_set_boundary_values(wenofd_solver *s, const double *host_table) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_table) return fail(WENOFD_BAD_ARG, "null table");
+  CUDA_TRY(cudaSetDevice(s->device));
+  const size_t n = 8 * size_t(s->g.nxt) + 8 * size_t(s->g.nyt);
+  CUDA_TRY(cudaMemcpyAsync(s->special, host_table, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   return sync(s);
 }
 

@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
         for name in ("wenofd_initialize", "wenofd_fill_boundary"):
             getattr(L, name).argtypes = [H]
         for name in ("wenofd_set_state", "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux",
+                     "wenofd_set_boundary_values",
                      "wenofd_calc_dt", "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums"):
             getattr(L, name).argtypes = [H, P]
         L.wenofd_set_state_device.argtypes = [H, C.c_void_p]
@@ -86,7 +87,7 @@ def lib() -> C.CDLL:
                   "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux", "wenofd_calc_dt",
                   "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_set_state_device",
                   "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
-                  "wenofd_time_stages", "wenofd_calc_dt_noalloc"):
+                  "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -171,6 +172,12 @@ class Solver:
     def set_time(self, now: float) -> None:
         _check(lib().wenofd_set_time(self._h, now))
 
+    def set_boundary_values(self, table: np.ndarray) -> None:
+        table = np.ascontiguousarray(table, dtype=np.float64)
+        if table.size != 8 * (self.nx + 8) + 8 * (self.ny + 8):
+            raise ValueError("SPECIAL table size mismatch")
+        _check(lib().wenofd_set_boundary_values(self._h, _dptr(table)))
+
     def fill_boundary(self) -> None:
         _check(lib().wenofd_fill_boundary(self._h))
 
@@ -226,5 +233,5 @@ EXPORTED = [
     "wenofd_set_state_device", "wenofd_get_state_device", "wenofd_get_state_ghosted", "wenofd_set_time",
     "wenofd_fill_boundary", "wenofd_get_flux", "wenofd_calc_dt", "wenofd_rk_step", "wenofd_step",
     "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
-    "wenofd_calc_dt_noalloc",
+    "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
 ]

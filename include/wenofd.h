@@ -72,7 +72,10 @@ const char *wenofd_version(void);
  * TESTCASE, ELEMNUMX, ELEMNUMY, RKMETH, CFL, SCHEME (src/WENOFD.cpp:24-40).
  * Optional keys the reference does not have: PRECISION (0 FP64, 1 FP32),
  * SEED (seeded cases), TEND (overrides equation->outputtime), DEVICE,
- * TILE_I (stage-kernel tile height; 0 = default). */
+ * TILE_I (stage-kernel tile height; 0 = default), and overrides of the
+ * EulerEquation members the reference's callers may set on their equation
+ * object (utils/equations.hpp:58-70): XL, XR, YL, YR, GAMMA, BC_LEFT,
+ * BC_RIGHT, BC_BOTTOM, BC_TOP (BOUNDARYTYPE values), GRAVITY (0/1). */
 int wenofd_create(const char *const *keys, const char *const *values, int n, wenofd_solver **out);
 /* Same, reading a config.cfg file with the reference's parser semantics
  * (`key = value` lines, `#` comments, trimmed spaces and '\r'). */
@@ -95,6 +98,14 @@ int wenofd_get_state_device(wenofd_solver *s, double *dev_state);
 /* Full state including the 4 ghost layers, [4][NX+8][NY+8] (host). */
 int wenofd_get_state_ghosted(wenofd_solver *s, double *host_full);
 int wenofd_set_time(wenofd_solver *s, double now);
+
+/* Values of SPECIAL boundaries (getU0 at fixed boundary nodes,
+ * src/WENOFD.cpp:1045-1058, 1092-1102, 1138-1149) for callers with their own
+ * initial condition.  Table of 8*(NX+8) + 8*(NY+8) doubles, each block
+ * r-major: bottom per ei at node (ei, 4); top per ei at (ei, NY+3); left per
+ * ej at (4, ej); right per ej at (NX+4, ej) -- the first ghost column, as the
+ * reference uses (line 1144).  ei, ej count the 4 ghost nodes. */
+int wenofd_set_boundary_values(wenofd_solver *s, const double *host_table);
 
 /* exchangeGhostCellsValue + setBoundary (src/WENOFD.cpp:850-929, 998-1159)
  * on the current state, in place. */

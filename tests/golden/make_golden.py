@@ -112,9 +112,36 @@ def run_ref(workdir: str, mode: str, testcase: int, nx: int, ny: int, scheme: in
     return res
 
 
+# CWENOFD::run of the reference, unchanged (mode fullrun): its output files
+# pin the drop-in host class's writers (outputAve, outputError,
+# outputAccuracy).
+OUTPUT_CASES = [("ref_output_smooth_16x12", "TESTCASE = 0\nELEMNUMX = 16\nELEMNUMY = 12\nRKMETH = 2\n"
+                 "CFL = 0.6\nSCHEME = 1\n")]
+
+
+def make_output_goldens() -> None:
+    import glob
+    import shutil
+    for name, cfg in OUTPUT_CASES:
+        dst = os.path.join(HERE, name)
+        os.makedirs(dst, exist_ok=True)
+        with tempfile.TemporaryDirectory() as wd:
+            with open(os.path.join(wd, "config.cfg"), "w") as f:
+                f.write(cfg)
+            r = subprocess.run([REF_BIN, "config.cfg", "fullrun", "out"], cwd=wd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(r.stderr[-2000:])
+            (run_dir,) = glob.glob(os.path.join(wd, "output", "*_SMOOTH_*"))
+            for fn in ("solution_initial.plt", "solution_final.plt", "error_final.plt", "accuracy_final.csv"):
+                shutil.copy(os.path.join(run_dir, fn), os.path.join(dst, fn))
+            shutil.copy(os.path.join(wd, "config.cfg"), os.path.join(dst, "config.cfg"))
+        print(f"{name}: reference output files")
+
+
 def main() -> None:
     if not os.path.exists(REF_BIN):
         sys.exit("build the reference first: make -C oracle ref")
+    make_output_goldens()
     for (name, mode, tc, nx, ny, sch, rk, cfl, seed, steps, t_end) in CASES:
         with tempfile.TemporaryDirectory() as wd:
             res = run_ref(wd, mode, tc, nx, ny, sch, rk, cfl, seed, steps, t_end)
