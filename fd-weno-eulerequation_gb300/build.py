@@ -37,6 +37,7 @@ CUDA_UNITS = {
     "stage_fp32.cu": [],
     "aux_kernels.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "learned.cu": ["-fmad=false"],
 }
 CXX_UNITS = ["capi.cpp", "cases.cpp"]
 

@@ -41,6 +41,12 @@ struct wenofd_solver {
   Ctrl *ctrl = nullptr;
   Ctrl *ctrl_host = nullptr;    // pinned mirror
   double *red_host = nullptr;   // pinned, 4 doubles
+  // learned form (PRECISION 2)
+  unsigned char *flags = nullptr;  // [nxt][pitch], ghosts 1
+  void *ind_weights = nullptr;     // packed BF16 indicator weights
+  int *ind_error = nullptr;
+  float ind_logit_threshold = 0.0f;
+  bool ind_ready = false;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   long long graph_kernels = 0;  // kernel nodes in the graph
@@ -135,9 +141,17 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   args.dt = &s->ctrl->dt;
   args.active = &s->ctrl->active;
   args.mode = mode;
+  args.flags = s->precision == WENOFD_LEARNED ? s->flags : nullptr;
   CUDA_TRY(wenofd::launch_bc_fill(s->g, const_cast<double *>(in), s->special, &s->ctrl->active, s->stream));
   s->launches += 2;
-  if (s->precision == WENOFD_FP32) {
+  // The learned form classifies the nodes once per step, on the stage-1
+  // input (ghosts just filled); all stages of the step route with those flags.
+  if (s->precision == WENOFD_LEARNED && in == s->S && un == s->S && s->ind_ready) {
+    CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
+                                      &s->ctrl->active, s->stream));
+    s->launches += 1;
+  }
+  if (s->precision != WENOFD_FP64) {
     CUDA_TRY(wenofd::launch_stage_fp32(s->g, args, s->scheme, s->tile_i, s->stream));
   } else {
     CUDA_TRY(wenofd::launch_stage_fp64(s->g, args, s->scheme, s->tile_i, s->stream));
@@ -217,6 +231,9 @@ void release(wenofd_solver *s) {
   cudaFree(s->partials);
   cudaFree(s->red_out);
   cudaFree(s->ctrl);
+  cudaFree(s->flags);
+  cudaFree(s->ind_weights);
+  cudaFree(s->ind_error);
   cudaFreeHost(s->ctrl_host);
   cudaFreeHost(s->red_host);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -252,7 +269,8 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   }
   if (rk < 0 || rk > 2) return fail(WENOFD_BAD_CONFIG, "Error: Invalid Runge-Kutta method");
   if (scheme < 0 || scheme > 3) return fail(WENOFD_BAD_CONFIG, "the scheme is not supported");
-  if (precision < 0 || precision > 1) return fail(WENOFD_BAD_CONFIG, "PRECISION must be 0 (FP64) or 1 (FP32)");
+  if (precision < 0 || precision > 2)
+    return fail(WENOFD_BAD_CONFIG, "PRECISION must be 0 (FP64), 1 (FP32) or 2 (learned + FP32)");
   if (nx < 6 || ny < 6) return fail(WENOFD_BAD_CONFIG, "ELEMNUMX and ELEMNUMY must be at least 6");
   if (nx > 65536 || ny > 65536) return fail(WENOFD_BAD_CONFIG, "ELEMNUMX and ELEMNUMY must be at most 65536");
   if (!(cfl > 0.0)) return fail(WENOFD_BAD_CONFIG, "CFL must be positive");
@@ -321,6 +339,14 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
             cudaMalloc(&s->ctrl, sizeof(Ctrl)) == cudaSuccess &&
             cudaMallocHost(&s->ctrl_host, sizeof(Ctrl)) == cudaSuccess &&
             cudaMallocHost(&s->red_host, 4 * sizeof(double)) == cudaSuccess;
+  if (ok && precision == WENOFD_LEARNED) {
+    const size_t fb = size_t(s->g.nxt) * s->g.pitch;
+    ok = cudaMalloc(&s->flags, fb) == cudaSuccess &&
+         cudaMalloc(&s->ind_weights, wenofd::indicator_weights_bytes()) == cudaSuccess &&
+         cudaMalloc(&s->ind_error, sizeof(int)) == cudaSuccess &&
+         cudaMemsetAsync(s->flags, 1, fb, s->stream) == cudaSuccess &&
+         cudaMemsetAsync(s->ind_error, 0, sizeof(int), s->stream) == cudaSuccess;
+  }
   if (!ok) {
     cudaGetLastError();
     return bail(fail(WENOFD_CUDA_ERROR, "device allocation failed"));
@@ -593,6 +619,11 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
     s->launches += s->graph_kernels;
     if (int rc = read_ctrl(s)) return rc;
     const Ctrl &c = *s->ctrl_host;
+    if (s->ind_error) {
+      int err = 0;
+      CUDA_TRY(cudaMemcpy(&err, s->ind_error, sizeof(int), cudaMemcpyDeviceToHost));
+      if (err) return fail(WENOFD_TIMEOUT, "indicator kernel: a tensor-core completion wait gave up");
+    }
     if (c.error) {
       if (steps_done) *steps_done = c.steps - start;
       return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
@@ -638,8 +669,9 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
   CUDA_TRY(cudaEventRecord(e0, s->stream));
   for (int r = 0; r < reps; ++r)
     for (const St &x : st) {
-      StageArgs a{x.in, x.un, x.out, x.a, x.b, x.c, &s->ctrl->dt, &s->ctrl->active, wenofd::kModeRK};
-      cudaError_t e = s->precision == WENOFD_FP32 ? wenofd::launch_stage_fp32(s->g, a, s->scheme, s->tile_i, s->stream)
+      StageArgs a{x.in, x.un, x.out, x.a, x.b, x.c, &s->ctrl->dt, &s->ctrl->active, wenofd::kModeRK,
+                  s->precision == WENOFD_LEARNED ? s->flags : nullptr};
+      cudaError_t e = s->precision != WENOFD_FP64 ? wenofd::launch_stage_fp32(s->g, a, s->scheme, s->tile_i, s->stream)
                                                   : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
       CUDA_TRY(e);
       s->launches += 1;
@@ -652,6 +684,49 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
   cudaEventDestroy(e1);
   *ms_per_launch = double(ms) / (double(reps) * st.size());
   return WENOFD_OK;
+}
+
+int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float threshold) {
+  if (int rc = check_handle(s)) return rc;
+  if (s->precision != WENOFD_LEARNED) return fail(WENOFD_BAD_CONFIG, "the indicator needs PRECISION = 2");
+  if (!host_params || !(threshold > 0.0f) || !(threshold < 1.0f)) return fail(WENOFD_BAD_ARG, "bad indicator arguments");
+  CUDA_TRY(cudaSetDevice(s->device));
+  std::vector<unsigned char> packed(wenofd::indicator_weights_bytes());
+  wenofd::pack_indicator_weights(host_params, packed.data());
+  CUDA_TRY(cudaMemcpyAsync(s->ind_weights, packed.data(), packed.size(), cudaMemcpyHostToDevice, s->stream));
+  s->ind_logit_threshold = std::log(threshold / (1.0f - threshold));
+  if (int rc = sync(s)) return rc;
+  s->ind_ready = true;
+  return WENOFD_OK;
+}
+
+int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_flags) return fail(WENOFD_BAD_ARG, "null flags");
+  if (s->precision != WENOFD_LEARNED || !s->ind_ready)
+    return fail(WENOFD_BAD_CONFIG, "no indicator loaded (PRECISION = 2 and wenofd_set_indicator)");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
+  CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
+                                    nullptr, s->stream));
+  s->launches += 3;
+  CUDA_TRY(cudaMemcpy2DAsync(host_flags, s->ny, s->flags + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost,
+                             s->g.pitch, s->ny, s->nx, cudaMemcpyDeviceToHost, s->stream));
+  int err = 0;
+  CUDA_TRY(cudaMemcpyAsync(&err, s->ind_error, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  if (int rc = sync(s)) return rc;
+  if (err) return fail(WENOFD_TIMEOUT, "indicator kernel: a tensor-core completion wait gave up");
+  return WENOFD_OK;
+}
+
+int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *dev_labels) {
+  if (int rc = check_handle(s)) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
+  if (dev_features) CUDA_TRY(wenofd::launch_features(s->g, s->S, dev_features, s->stream));
+  if (dev_labels) CUDA_TRY(wenofd::launch_labels(s->g, s->S, dev_labels, s->stream));
+  return sync(s);
 }
 
 int wenofd_conservation_sums(wenofd_solver *s, double out[4]) {

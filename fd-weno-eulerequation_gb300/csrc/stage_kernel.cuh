@@ -31,7 +31,18 @@ struct StageSmem {
   static constexpr size_t bytes = sizeof(T) * (size_t(kU) + 2 * kSplit + kFace);
 };
 
-template <typename T, int SCHEME, int TI, int TJ, int NT>
+// Linear fifth-order upwind flux of one component: WENO with its weights
+// frozen at (0.1, 0.6, 0.3), on F+ at nodes face-3..face+1 (a..e) and on F-
+// mirrored (nodes face+2..face-2): (2a - 13b + 47c + 27d - 3e) / 60 each.
+template <typename T>
+__device__ __forceinline__ T linear_upwind(const T *P, const T *M, int ss) {
+  const T c0 = T(2.0 / 60.0), c1 = T(-13.0 / 60.0), c2 = T(47.0 / 60.0), c3 = T(27.0 / 60.0), c4 = T(-3.0 / 60.0);
+  const T plus = c0 * P[0] + c1 * P[ss] + c2 * P[2 * ss] + c3 * P[3 * ss] + c4 * P[4 * ss];
+  const T minus = c0 * M[4 * ss] + c1 * M[3 * ss] + c2 * M[2 * ss] + c3 * M[ss] + c4 * M[0];
+  return plus + minus;
+}
+
+template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
 __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
   using S = StageSmem<T, TI, TJ>;
@@ -41,6 +52,13 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   T *Fp = Us + S::kU;
   T *Fm = Fp + S::kSplit;
   T *Hf = Fm + S::kSplit;
+  // routed form: node flags of the tile with a 2-node halo, and the list of
+  // faces that need WENO
+  constexpr int FI = TI + 4, FJ = TJ + 4;
+  constexpr int kMaxFaces = (TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1);
+  __shared__ unsigned char sflag[ROUTE ? FI * FJ : 1];
+  __shared__ short slist[ROUTE ? kMaxFaces : 1];
+  __shared__ int scount;
 
   const int i0 = blockIdx.y * TI;  // first interior node of the tile (0-based)
   const int j0 = blockIdx.x * TJ;
@@ -56,6 +74,14 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     T val = T(0);
     if (ei < g.nxt && ej < g.nyt) val = T(a.uin[r * g.plane + (long long)ei * g.pitch + ej]);
     Us[t] = val;
+  }
+  if constexpr (ROUTE) {
+    for (int t = threadIdx.x; t < FI * FJ; t += NT) {
+      const int fi = t / FJ, fj = t - (t / FJ) * FJ;
+      const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;  // nodes i0-2+fi, j0-2+fj
+      sflag[t] = (ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
+    }
+    if (threadIdx.x == 0) scount = 0;
   }
   __syncthreads();
 
@@ -74,18 +100,46 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   }
   __syncthreads();
   // x faces f = 0..TI: face between tile nodes f-1 and f (halo rows f+2, f+3)
-  for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
-    const int f = t / TJ, j = t - f * TJ;
-    if (i0 + f > g.nx || j0 + j >= g.ny) continue;
-    T um[4], u0[4], out[4];
+  if constexpr (ROUTE) {
+    for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
+      const int f = t / TJ, j = t - f * TJ;
+      if (i0 + f > g.nx || j0 + j >= g.ny) continue;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
-      u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
+      for (int r = 0; r < 4; ++r)
+        Hf[(r * (TI + 1) + f) * TJ + j] = linear_upwind(Fp + (r * HI + f) * TJ + j, Fm + (r * HI + f + 1) * TJ + j, TJ);
+      // nodes f-2 .. f+1 of the tile = flag rows f .. f+3
+      const unsigned char *fl = sflag + f * FJ + (j + 2);
+      if (fl[0] | fl[FJ] | fl[2 * FJ] | fl[3 * FJ]) slist[atomicAdd(&scount, 1)] = short(t);
     }
-    face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
+    __syncthreads();
+    const int nw = scount;
+    for (int q = threadIdx.x; q < nw; q += NT) {
+      const int t = slist[q];
+      const int f = t / TJ, j = t - f * TJ;
+      T um[4], u0[4], out[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
+      for (int r = 0; r < 4; ++r) {
+        um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
+        u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
+      }
+      face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
+    }
+  } else {
+    for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
+      const int f = t / TJ, j = t - f * TJ;
+      if (i0 + f > g.nx || j0 + j >= g.ny) continue;
+      T um[4], u0[4], out[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
+        u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
+      }
+      face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
+    }
   }
   __syncthreads();
 
@@ -105,6 +159,9 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
       }
     }
   }
+  if constexpr (ROUTE) {
+    if (threadIdx.x == 0) scount = 0;
+  }
   __syncthreads();
 
   // --- y sweep: split fluxes of tile rows, halo columns 0..HJ-1
@@ -121,18 +178,46 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
-    const int i = t / (TJ + 1), f = t - i * (TJ + 1);
-    if (i0 + i >= g.nx || j0 + f > g.ny) continue;
-    T um[4], u0[4], out[4];
+  if constexpr (ROUTE) {
+    for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
+      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
+      if (i0 + i >= g.nx || j0 + f > g.ny) continue;
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
-      u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
+      for (int r = 0; r < 4; ++r)
+        Hf[(r * TI + i) * (TJ + 1) + f] = linear_upwind(Fp + (r * TI + i) * HJ + f, Fm + (r * TI + i) * HJ + f + 1, 1);
+      // nodes f-2 .. f+1 along y = flag columns f .. f+3 of flag row i+2
+      const unsigned char *fl = sflag + (i + 2) * FJ + f;
+      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount, 1)] = short(t);
     }
-    face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
+    __syncthreads();
+    const int nw = scount;
+    for (int q = threadIdx.x; q < nw; q += NT) {
+      const int t = slist[q];
+      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
+      T um[4], u0[4], out[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
+      for (int r = 0; r < 4; ++r) {
+        um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
+        u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
+      }
+      face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
+    }
+  } else {
+    for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
+      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
+      if (i0 + i >= g.nx || j0 + f > g.ny) continue;
+      T um[4], u0[4], out[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
+        u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
+      }
+      face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
+    }
   }
   __syncthreads();
 
@@ -171,17 +256,17 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
 
 // Host-side launcher for one precision: picks the kernel instance for the
 // scheme and tile height, sets its shared-memory size, launches it.
-template <typename T, int TI, int NT>
+template <typename T, int TI, int NT, bool ROUTE = false>
 cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cudaStream_t s) {
   constexpr int TJ = 32;
   using Sm = StageSmem<T, TI, TJ>;
   const dim3 grid((g.ny + TJ - 1) / TJ, (g.nx + TI - 1) / TI);
   void (*fn)(Geom, StageArgs) = nullptr;
   switch (scheme) {
-    case kWenoJS: fn = k_stage<T, kWenoJS, TI, TJ, NT>; break;
-    case kWenoZ: fn = k_stage<T, kWenoZ, TI, TJ, NT>; break;
-    case kWenoZP: fn = k_stage<T, kWenoZP, TI, TJ, NT>; break;
-    case kWenoZPI: fn = k_stage<T, kWenoZPI, TI, TJ, NT>; break;
+    case kWenoJS: fn = k_stage<T, kWenoJS, TI, TJ, NT, ROUTE>; break;
+    case kWenoZ: fn = k_stage<T, kWenoZ, TI, TJ, NT, ROUTE>; break;
+    case kWenoZP: fn = k_stage<T, kWenoZP, TI, TJ, NT, ROUTE>; break;
+    case kWenoZPI: fn = k_stage<T, kWenoZPI, TI, TJ, NT, ROUTE>; break;
     default: return cudaErrorInvalidValue;
   }
   // The dynamic shared-memory limit is a per-device function attribute: set

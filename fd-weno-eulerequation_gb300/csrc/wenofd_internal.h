@@ -53,15 +53,28 @@ struct StageArgs {
   const double *dt;    // device pointer (Ctrl::dt)
   const int *active;   // device pointer (Ctrl::active); 0 -> return
   int mode;            // kModeRK or kModeRHS (uout = rhs)
+  // Learned form only: per-node troubled-cell flags, [nxt][pitch] bytes,
+  // ghosts 1.  A face takes characteristic WENO-Z when any of the four nodes
+  // around it along its line is flagged, else the linear upwind flux.
+  const unsigned char *flags = nullptr;
 };
 enum { kModeRK = 0, kModeRHS = 1 };
 
 Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lambda, int bc_left,
                int bc_right, int bc_y, int gravity);
 
-// stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form)
+// stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form,
+// routed by a.flags when it is set)
 cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
 cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
+
+// learned.cu: indicator features, labels, tensor-core inference
+size_t indicator_weights_bytes();
+void pack_indicator_weights(const float *params, void *host_out);
+cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStream_t s);
+cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, cudaStream_t s);
+cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
+                             unsigned char *flags, int *error, const int *active, cudaStream_t s);
 
 // aux_kernels.cu
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s);

@@ -21,7 +21,8 @@ PKG = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "_build", "libwenofd.so")
 
 OK, BAD_CONFIG, CUDA_ERROR, NAN_DT, TIMEOUT, BAD_ARG, NO_EXACT = range(7)
-FP64, FP32 = 0, 1
+FP64, FP32, LEARNED = 0, 1, 2
+MLP_INPUTS, MLP_PARAMS = 50, 2721
 SMOOTH, RIEMANN1, RIEMANN2, RTI, RIEMANN_SEEDED, SHEAR = range(6)
 WENOJS, WENOZ, WENOZP, WENOZPI = range(4)
 RK1, RK2, RK3 = range(3)
@@ -79,6 +80,15 @@ def lib() -> C.CDLL:
         L.wenofd_rk_step.argtypes = [H, C.c_double]
         L.wenofd_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
         L.wenofd_time_stages.argtypes = [H, C.c_int, P]
+        VP = C.c_void_p
+        L.wenofd_set_indicator.argtypes = [H, C.POINTER(C.c_float), C.c_float]
+        L.wenofd_indicator_flags.argtypes = [H, C.POINTER(C.c_ubyte)]
+        L.wenofd_indicator_data.argtypes = [H, VP, VP]
+        L.wenofd_mlp_forward.argtypes = [VP, VP, C.c_longlong, VP, VP]
+        L.wenofd_mlp_backward.argtypes = [VP, VP, VP, C.c_longlong, VP, VP, VP]
+        L.wenofd_mlp_adam.argtypes = [VP, VP, VP, VP, C.c_int, C.c_float, VP]
+        L.wenofd_mlp_train.argtypes = [VP, VP, VP, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong,
+                                       C.POINTER(C.c_float), VP]
         D = C.c_double
         L.wenofd_calc_dt_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, D, D, D, D, D, D, C.c_void_p,
                                              C.c_void_p]
@@ -87,7 +97,9 @@ def lib() -> C.CDLL:
                   "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux", "wenofd_calc_dt",
                   "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_set_state_device",
                   "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
-                  "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values"):
+                  "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
+                  "wenofd_set_indicator", "wenofd_indicator_flags", "wenofd_indicator_data", "wenofd_mlp_forward",
+                  "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -221,6 +233,21 @@ class Solver:
         _check(lib().wenofd_time_stages(self._h, reps, _dptr(ms)))
         return float(ms[0])
 
+    def set_indicator(self, params: np.ndarray, threshold: float = 0.5) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != MLP_PARAMS:
+            raise ValueError(f"expected {MLP_PARAMS} parameters")
+        _check(lib().wenofd_set_indicator(self._h, p.ctypes.data_as(C.POINTER(C.c_float)), threshold))
+
+    def indicator_flags(self) -> np.ndarray:
+        out = np.zeros((self.nx, self.ny), dtype=np.uint8)
+        _check(lib().wenofd_indicator_flags(self._h, out.ctypes.data_as(C.POINTER(C.c_ubyte))))
+        return out
+
+    def indicator_data(self, dev_features: int | None, dev_labels: int | None) -> None:
+        """Features [NX*NY][50] float32 / labels [NX*NY] uint8 into device buffers."""
+        _check(lib().wenofd_indicator_data(self._h, C.c_void_p(dev_features or 0), C.c_void_p(dev_labels or 0)))
+
     def conservation_sums(self) -> np.ndarray:
         out = np.zeros(4)
         _check(lib().wenofd_conservation_sums(self._h, _dptr(out)))
@@ -233,5 +260,30 @@ EXPORTED = [
     "wenofd_set_state_device", "wenofd_get_state_device", "wenofd_get_state_ghosted", "wenofd_set_time",
     "wenofd_fill_boundary", "wenofd_get_flux", "wenofd_calc_dt", "wenofd_rk_step", "wenofd_step",
     "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
-    "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
+    "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values", "wenofd_set_indicator", "wenofd_indicator_flags",
+    "wenofd_indicator_data", "wenofd_mlp_forward", "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train",
 ]
+
+
+def mlp_forward(params_ptr: int, x_ptr: int, n: int, logits_ptr: int, stream: int = 0) -> None:
+    _check(lib().wenofd_mlp_forward(C.c_void_p(params_ptr), C.c_void_p(x_ptr), n, C.c_void_p(logits_ptr),
+                                    C.c_void_p(stream)))
+
+
+def mlp_backward(params_ptr: int, x_ptr: int, y_ptr: int, n: int, grad_ptr: int, loss_ptr: int,
+                 stream: int = 0) -> None:
+    _check(lib().wenofd_mlp_backward(C.c_void_p(params_ptr), C.c_void_p(x_ptr), C.c_void_p(y_ptr), n,
+                                     C.c_void_p(grad_ptr), C.c_void_p(loss_ptr), C.c_void_p(stream)))
+
+
+def mlp_adam(params_ptr: int, grad_ptr: int, m_ptr: int, v_ptr: int, step: int, lr: float, stream: int = 0) -> None:
+    _check(lib().wenofd_mlp_adam(C.c_void_p(params_ptr), C.c_void_p(grad_ptr), C.c_void_p(m_ptr),
+                                 C.c_void_p(v_ptr), step, lr, C.c_void_p(stream)))
+
+
+def mlp_train(params_ptr: int, x_ptr: int, y_ptr: int, n: int, epochs: int, batch: int, lr: float, seed: int,
+              stream: int = 0) -> np.ndarray:
+    losses = np.zeros(epochs, dtype=np.float32)
+    _check(lib().wenofd_mlp_train(C.c_void_p(params_ptr), C.c_void_p(x_ptr), C.c_void_p(y_ptr), n, epochs, batch,
+                                  lr, seed, losses.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(stream)))
+    return losses

@@ -40,8 +40,11 @@ enum wenofd_status {
 
 /* Arithmetic of the flux / reconstruction kernels.  FP64 reproduces the
  * reference bit for bit.  FP32 keeps state, RK sums, the time-step reduction
- * and all norms in FP64 and evaluates fluxes and reconstruction in FP32. */
-enum wenofd_precision { WENOFD_FP64 = 0, WENOFD_FP32 = 1 };
+ * and all norms in FP64 and evaluates fluxes and reconstruction in FP32.
+ * LEARNED is FP32 plus the learned troubled-cell indicator: each step a
+ * tensor-core MLP flags nodes, and only faces near flagged nodes take
+ * characteristic WENO; the others take the linear fifth-order upwind flux. */
+enum wenofd_precision { WENOFD_FP64 = 0, WENOFD_FP32 = 1, WENOFD_LEARNED = 2 };
 
 /* Test cases: TESTCASETYPE (utils/equations.hpp:30-36) plus two seeded ones. */
 enum wenofd_testcase {
@@ -142,6 +145,41 @@ int wenofd_conservation_sums(wenofd_solver *s, double out[4]);
  * duration of one stage-kernel launch in milliseconds.  It advances the
  * state; callers re-upload a state afterwards. */
 int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch);
+
+/* ---- Learned troubled-cell indicator (no counterpart in the reference) ----
+ * Network: 50 inputs (5x5 windows of density and pressure, each normalised
+ * as (v - v_centre) / max|v - v_centre|, zero when that range is <= 1e-2 of
+ * |v_centre|) -> 32 -> 32 -> 1, GELU (tanh form) hidden layers, sigmoid
+ * output.  Parameters are WENOFD_MLP_PARAMS floats: W1[32][50], b1[32],
+ * W2[32][32], b2[32], w3[32], b3. */
+#define WENOFD_MLP_INPUTS 50
+#define WENOFD_MLP_PARAMS 2721
+
+/* Load trained parameters (host, FP32; converted to BF16 for the tensor
+ * cores) into a PRECISION = 2 solver; nodes whose predicted probability
+ * exceeds `threshold` are flagged.  Without it every face takes WENO. */
+int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float threshold);
+/* Run the indicator on the current state; flags [NX][NY] bytes to the host. */
+int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags);
+/* Training data of the current state: features [NX*NY][50] float and labels
+ * [NX*NY] bytes (1 where WENO-Z's nonlinear weights differ from the linear
+ * ones by more than 1e-2 on a non-flat stencil at any of the node's four
+ * faces), device pointers; either may be NULL. */
+int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *dev_labels);
+/* FP32 training kernels on device buffers (stream-ordered):
+ *   forward: logits[n] of samples x[n][50];
+ *   backward: mean binary cross-entropy of logits vs y[n] (0/1) into *loss and
+ *             its gradient into grad[WENOFD_MLP_PARAMS] (both overwritten);
+ *   adam: one Adam step (beta 0.9 / 0.999, eps 1e-8), step counts from 1;
+ *   train: epochs of shuffled mini-batches of backward + adam, the mean loss
+ *          of each epoch to host_epoch_loss[epochs] (may be NULL). */
+int wenofd_mlp_forward(const float *dev_params, const float *dev_x, long long n, float *dev_logits, void *stream);
+int wenofd_mlp_backward(const float *dev_params, const float *dev_x, const float *dev_y, long long n,
+                        float *dev_grad, float *dev_loss, void *stream);
+int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *dev_m, float *dev_v, int step, float lr,
+                    void *stream);
+int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs, int batch,
+                     float lr, unsigned long long seed, float *host_epoch_loss, void *stream);
 
 /* No counterpart in the reference.  calculateDeltaT (src/WENOFD.cpp:398-452
  * arithmetic, bit for bit) of a caller-owned device state, for callers that

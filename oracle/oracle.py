@@ -95,6 +95,8 @@ def lib() -> C.CDLL:
                               C.POINTER(C.c_long), P, C.c_long]
         L.orc_error_norms.argtypes = [C.POINTER(Grid), P, D, P]
         L.orc_conservation_sums.argtypes = [C.POINTER(Grid), P, P]
+        L.orc_cell_features.argtypes = [C.POINTER(Grid), P, C.POINTER(C.c_float)]
+        L.orc_cell_labels.argtypes = [C.POINTER(Grid), P, C.POINTER(C.c_ubyte)]
         _lib = L
     return _lib
 
@@ -189,6 +191,20 @@ class Problem:
     def error_norms(self, t: float | None = None) -> np.ndarray:
         out = np.zeros(3)
         lib().orc_error_norms(C.byref(self.grid), _p(self.U), self.now if t is None else t, _p(out))
+        return out
+
+    def cell_features(self) -> np.ndarray:
+        """(NX*NY, 50) float32 indicator features of the current state (fills ghosts)."""
+        self.fill_boundary()
+        out = np.zeros((self.nx * self.ny, 50), dtype=np.float32)
+        lib().orc_cell_features(C.byref(self.grid), _p(self.U), out.ctypes.data_as(C.POINTER(C.c_float)))
+        return out
+
+    def cell_labels(self) -> np.ndarray:
+        """(NX*NY,) uint8 WENO-Z weight-deviation labels of the current state."""
+        self.fill_boundary()
+        out = np.zeros(self.nx * self.ny, dtype=np.uint8)
+        lib().orc_cell_labels(C.byref(self.grid), _p(self.U), out.ctypes.data_as(C.POINTER(C.c_ubyte)))
         return out
 
     def conservation_sums(self) -> np.ndarray:

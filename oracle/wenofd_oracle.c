@@ -766,3 +766,111 @@ void orc_conservation_sums(const orc_grid *g, const double *U, double out[4]) {
     out[r] = s;
   }
 }
+
+/* ------------------------------------------- learned indicator (own spec) */
+
+static float feat_pressure(float gamma, const float q[4]) {
+  const float u = q[1] / q[0], v = q[2] / q[0];
+  return (gamma - 1.0f) * (q[3] - 0.5f * q[0] * (u * u + v * v));
+}
+
+static void normalise_window(const float w[25], float out[25]) {
+  const float c = w[12];
+  float R = 0.0f;
+  for (int k = 0; k < 25; ++k) {
+    const float d = fabsf(w[k] - c);
+    if (d > R) R = d;
+  }
+  if (R <= 1e-2f * (fabsf(c) + 1e-12f)) {
+    for (int k = 0; k < 25; ++k) out[k] = 0.0f;
+    return;
+  }
+  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) / R;
+}
+
+void orc_cell_features(const orc_grid *g, const double *U, float *features) {
+  const float gam = (float)g->gamma;
+  for (int i = 0; i < g->nx; ++i)
+    for (int j = 0; j < g->ny; ++j) {
+      float wr[25], wp[25];
+      for (int a = 0; a < 5; ++a)
+        for (int b = 0; b < 5; ++b) {
+          float q[4];
+          for (int r = 0; r < 4; ++r) q[r] = (float)AT(g, U, r, ORC_NG + i + a - 2, ORC_NG + j + b - 2);
+          wr[a * 5 + b] = q[0];
+          wp[a * 5 + b] = feat_pressure(gam, q);
+        }
+      float *o = features + ((size_t)i * g->ny + j) * 50;
+      normalise_window(wr, o);
+      normalise_window(wp, o + 25);
+    }
+}
+
+/* max |w_k - d_k| of WENO-Z for one characteristic field and side; 0 when
+ * the stencil's range is <= 1e-2 of `scale` (the largest characteristic
+ * magnitude at the face): such a stencil changes the flux negligibly
+ * whatever its weights. */
+static double face_side_deviation(const double v[5], double scale) {
+  double lo = v[0], hi = v[0];
+  for (int s = 1; s < 5; ++s) {
+    if (v[s] < lo) lo = v[s];
+    if (v[s] > hi) hi = v[s];
+  }
+  if (hi - lo <= 1e-2 * scale) return 0.0;
+  double w[3];
+  orc_wenoz_weights(v[0], v[1], v[2], v[3], v[4], w);
+  const double d[3] = {0.1, 0.6, 0.3};
+  double dev = 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (fabs(w[k] - d[k]) > dev) dev = fabs(w[k] - d[k]);
+  return dev;
+}
+
+/* Face between nodes (ei-1, ej) and (ei, ej) (dir 0) or (ei, ej-1) and
+ * (ei, ej) (dir 1), full-array indices. */
+static double face_deviation(const orc_grid *g, const double *U, int dir, int ei, int ej) {
+  const int di = dir == 0 ? 1 : 0, dj = dir == 0 ? 0 : 1;
+  double um[4], u0[4], ave[4], L[16], R[16], fp[6][4], fm[6][4];
+  for (int r = 0; r < 4; ++r) {
+    um[r] = AT(g, U, r, ei - di, ej - dj);
+    u0[r] = AT(g, U, r, ei, ej);
+    ave[r] = 0.5 * (um[r] + u0[r]);
+  }
+  orc_eigen_lr(dir, g->gamma, ave, L, R);
+  for (int s = 0; s < 6; ++s) { /* nodes face-3 .. face+2 */
+    double q[4];
+    for (int r = 0; r < 4; ++r) q[r] = AT(g, U, r, ei + (s - 3) * di, ej + (s - 3) * dj);
+    orc_flux_split(dir, g->gamma, q, fm[s], fp[s]);
+  }
+  double vp[4][5], vm[4][5], scale = 0.0;
+  for (int k = 0; k < 4; ++k)
+    for (int s = 0; s < 5; ++s) {
+      vp[k][s] = L[k * 4 + 0] * fp[s][0] + L[k * 4 + 1] * fp[s][1] + L[k * 4 + 2] * fp[s][2] + L[k * 4 + 3] * fp[s][3];
+      vm[k][4 - s] = L[k * 4 + 0] * fm[s + 1][0] + L[k * 4 + 1] * fm[s + 1][1] + L[k * 4 + 2] * fm[s + 1][2] +
+                     L[k * 4 + 3] * fm[s + 1][3];
+      if (fabs(vp[k][s]) > scale) scale = fabs(vp[k][s]);
+      if (fabs(vm[k][4 - s]) > scale) scale = fabs(vm[k][4 - s]);
+    }
+  double dev = 0.0;
+  for (int k = 0; k < 4; ++k) {
+    const double a = face_side_deviation(vp[k], scale), b = face_side_deviation(vm[k], scale);
+    if (a > dev) dev = a;
+    if (b > dev) dev = b;
+  }
+  return dev;
+}
+
+void orc_cell_labels(const orc_grid *g, const double *U, unsigned char *labels) {
+  for (int i = 0; i < g->nx; ++i)
+    for (int j = 0; j < g->ny; ++j) {
+      const int ei = ORC_NG + i, ej = ORC_NG + j;
+      double dev = face_deviation(g, U, 0, ei, ej);
+      double d2 = face_deviation(g, U, 0, ei + 1, ej);
+      if (d2 > dev) dev = d2;
+      d2 = face_deviation(g, U, 1, ei, ej);
+      if (d2 > dev) dev = d2;
+      d2 = face_deviation(g, U, 1, ei, ej + 1);
+      if (d2 > dev) dev = d2;
+      labels[(size_t)i * g->ny + j] = dev > 1e-2;
+    }
+}

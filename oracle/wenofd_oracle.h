@@ -87,8 +87,21 @@ int orc_run(const orc_grid *g, int rk, double cfl, double *U, double *Un, double
             double t_end, long max_steps, long *steps, double *dts, long dts_cap);
 void orc_error_norms(const orc_grid *g, const double *U, double t, double out[3]);
 
-/* pieces for the learned troubled-cell indicator */
 void orc_conservation_sums(const orc_grid *g, const double *U, double out[4]);
+
+/* Learned troubled-cell indicator (no reference counterpart; these restate
+ * this project's own definitions, for checking the CUDA kernels):
+ *  features: per interior cell, the 5x5 windows of density and pressure,
+ *    each normalised as (v - v_centre) / max|v - v_centre| (all zero when
+ *    that range is <= 1e-2 (|v_centre| + 1e-12)); 50 floats, density first,
+ *    window row-major in (ei, ej).  Computed in FP32 from the FP32-rounded
+ *    state.  U must have its ghosts filled.
+ *  labels: 1 if, at any of the cell's four faces, for any characteristic
+ *    field and side, the WENO-Z nonlinear weights differ from (0.1, 0.6, 0.3)
+ *    by more than 1e-2 while that stencil's values vary by more than 1e-2
+ *    of the largest characteristic magnitude at the face.  FP64. */
+void orc_cell_features(const orc_grid *g, const double *U, float *features);
+void orc_cell_labels(const orc_grid *g, const double *U, unsigned char *labels);
 
 unsigned long long orc_splitmix64(unsigned long long *state);
 double orc_uniform01(unsigned long long *state);

@@ -1,0 +1,136 @@
+"""The learned troubled-cell indicator: features and labels against the
+oracle's restatement, the FP32 training kernels against a NumPy float64
+restatement, BF16 tensor-core inference against the FP32 forward, routing
+(all-WENO routing equals the FP32 form bit for bit), and the gain of a
+trained network over the method without it."""
+import numpy as np
+import pytest
+
+import mlp_oracle
+import oracle as orc
+import wenofd
+from wenofd import learned
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _riemann_state(n=48, m=40, steps=10, seed=3):
+    p = orc.Problem(orc.RIEMANN_SEEDED, n, m, orc.WENOZ, 2, 0.7, seed=seed)
+    p.run(max_steps=steps)
+    return p
+
+
+def test_features_and_labels_match_oracle():
+    p = _riemann_state()
+    with wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": p.nx, "ELEMNUMY": p.ny, "RKMETH": 2, "CFL": 0.7,
+                        "SCHEME": 1, "SEED": 3}) as s:
+        s.set_state(p.interior())
+        feat = torch.empty((p.nx * p.ny, 50), dtype=torch.float32, device="cuda")
+        lab = torch.empty(p.nx * p.ny, dtype=torch.uint8, device="cuda")
+        s.indicator_data(feat.data_ptr(), lab.data_ptr())
+        torch.cuda.synchronize()
+    f_ref, l_ref = p.cell_features(), p.cell_labels()
+    assert np.array_equal(feat.cpu().numpy(), f_ref)
+    assert np.array_equal(lab.cpu().numpy(), l_ref)
+    assert 0.05 < l_ref.mean() < 0.95
+
+
+def test_mlp_forward_backward_adam_match_numpy():
+    rng = np.random.default_rng(4)
+    n = 1000
+    X = rng.uniform(-1, 1, (n, 50)).astype(np.float32)
+    y = (rng.uniform(size=n) < 0.4).astype(np.float32)
+    P = mlp_oracle.init_params(7)
+    dP, dX, dy = (torch.from_numpy(a).cuda() for a in (P, X, y))
+    logits = torch.empty(n, device="cuda")
+    wenofd.mlp_forward(dP.data_ptr(), dX.data_ptr(), n, logits.data_ptr())
+    grad = torch.empty(wenofd.MLP_PARAMS, device="cuda")
+    loss = torch.empty(1, device="cuda")
+    wenofd.mlp_backward(dP.data_ptr(), dX.data_ptr(), dy.data_ptr(), n, grad.data_ptr(), loss.data_ptr())
+    torch.cuda.synchronize()
+    ref_logits, _ = mlp_oracle.forward(P, X)
+    ref_loss, ref_grad = mlp_oracle.loss_and_grad(P, X, y)
+    assert np.allclose(logits.cpu().numpy(), ref_logits, rtol=1e-4, atol=1e-4)
+    assert float(loss.cpu()[0]) == pytest.approx(ref_loss, rel=1e-5)
+    g = grad.cpu().numpy()
+    assert np.max(np.abs(g - ref_grad)) <= 1e-4 * np.max(np.abs(ref_grad)) + 1e-7
+    # one Adam step
+    m = torch.zeros_like(grad)
+    v = torch.zeros_like(grad)
+    wenofd.mlp_adam(dP.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(), 1, 1e-3)
+    torch.cuda.synchronize()
+    ref_p, _, _ = mlp_oracle.adam(P.astype(np.float64), g.astype(np.float64), 0.0, 0.0, 1, 1e-3)
+    assert np.allclose(dP.cpu().numpy(), ref_p, rtol=1e-5, atol=1e-6)
+
+
+def test_tensor_core_indicator_matches_fp32_forward():
+    p = _riemann_state(96, 72, 15, seed=9)
+    P = mlp_oracle.init_params(3)
+    P[2720] = 0.2  # b3
+    with wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": p.nx, "ELEMNUMY": p.ny, "RKMETH": 2, "CFL": 0.7,
+                        "SCHEME": 1, "SEED": 9, "PRECISION": wenofd.LEARNED}) as s:
+        s.set_state(p.interior())
+        s.set_indicator(P, 0.5)
+        flags = s.indicator_flags().ravel()
+    X = torch.from_numpy(p.cell_features()).cuda()
+    logits = learned.predict_logits(torch, P, X).cpu().numpy()
+    want = logits > 0.0
+    # BF16 operands can flip cells whose logit is within rounding of the threshold
+    close = np.abs(logits) < 0.05 * np.maximum(1.0, np.abs(logits).max())
+    assert np.array_equal(flags[~close].astype(bool), want[~close])
+    assert 0.01 < want.mean() < 0.99
+
+
+def _run(n, testcase, seed, precision, steps, params=None, threshold=0.5, init=None):
+    with wenofd.Solver({"TESTCASE": testcase, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7,
+                        "SCHEME": 1, "SEED": seed, "PRECISION": precision}) as s:
+        if init is None:
+            s.initialize()
+        else:
+            s.set_state(init)
+        if params is not None:
+            s.set_indicator(params, threshold)
+        s.advance(max_steps=steps)
+        flagged = float(s.indicator_flags().mean()) if params is not None else 1.0
+        return s.get_state(), flagged
+
+
+def _constant_net(b3):
+    P = np.zeros(wenofd.MLP_PARAMS, dtype=np.float32)
+    P[2720] = b3
+    return P
+
+
+def test_all_weno_routing_equals_fp32_form():
+    U32, _ = _run(128, 4, 5, wenofd.FP32, 12)
+    Uall, frac = _run(128, 4, 5, wenofd.LEARNED, 12, params=_constant_net(50.0))
+    assert frac == 1.0
+    assert np.array_equal(U32, Uall)
+
+
+def test_trained_indicator_gain_over_the_method_without_it():
+    """Train on solver-produced stencils (seeds other than the test seed),
+    then solve a seeded four-quadrant Riemann problem three ways against
+    plain FP64 WENO-Z: always linear (the method without the indicator),
+    learned routing, always WENO.  The network must catch the
+    discontinuities (recall) while sending most faces to the cheap flux."""
+    X, y = learned.generate_dataset(torch, runs=((4, 21), (4, 22), (5, 23)), n=256, snapshots=(20, 60, 120),
+                                    per_snapshot=40_000)
+    params, losses = learned.train(torch, X, y, epochs=12, batch=2048, lr=3e-3)
+    assert losses[-1] < 0.6 * losses[0]
+    recall, precision, _ = learned.recall_precision(torch, params, X, y, threshold=0.3)
+    assert recall > 0.9
+    n, steps, seed = 256, 80, 31
+    ref, _ = _run(n, 4, seed, wenofd.FP64, steps)
+    lin, f_lin = _run(n, 4, seed, wenofd.LEARNED, steps, params=_constant_net(-50.0))
+    lrn, f_lrn = _run(n, 4, seed, wenofd.LEARNED, steps, params=params, threshold=0.3)
+    weno, _ = _run(n, 4, seed, wenofd.FP32, steps)
+    err = lambda U: float(np.mean(np.abs(U[0] - ref[0]))) if np.all(np.isfinite(U)) else np.inf
+    e_lin, e_lrn, e_weno = err(lin), err(lrn), err(weno)
+    assert f_lin == 0.0
+    assert f_lrn < 0.6
+    assert e_lrn < 0.25 * e_lin
+    assert np.all(np.isfinite(lrn))
+    print(f"flagged {f_lrn:.3f}; L1 rho vs FP64 WENO-Z: linear {e_lin:.3e}, learned {e_lrn:.3e}, "
+          f"FP32 WENO {e_weno:.3e}; recall {recall:.3f} precision {precision:.3f}")
