@@ -27,11 +27,16 @@ __device__ __forceinline__ long long at(const Geom &g, int r, int ei, int ej) {
 //   SPECIAL      : initial-condition value at the boundary node (table)
 // The y direction uses the bottom condition on both sides (line 1009).
 // Corner ghosts (x ghost and y ghost at once) are never read by the sweeps
-// (lines 513-797) and are not written.
+// (lines 513-797) but are read by the indicator's 5x5 windows; they get the
+// reference's values: its y fill runs over every column, ghost columns
+// included, after the x exchange, and its x conditions then run over every
+// row, ghost rows included.  So a corner is the y rule applied to the
+// x-periodic source column (x periodic) or the x rule applied to the y ghost
+// of the interior source column (x not periodic).
 __global__ void k_bc_fill(Geom g, double *U, const double *special, const int *active) {
   if (active && *active == 0) return;
   const int nxg = 4 * g.nx, nyg = 4 * g.ny;
-  const int total = 2 * nyg + 2 * nxg;
+  const int total = 2 * nyg + 2 * nxg + 64;
   const int sx = kGhost, ex = kGhost + g.nx, sy = kGhost, ey = kGhost + g.ny;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     if (t < 2 * nyg) {  // x ghosts on interior rows
@@ -49,6 +54,30 @@ __global__ void k_bc_fill(Geom g, double *U, const double *special, const int *a
         else v = U[at(g, r, src, ej)];
         if (bc == kSlip && r == 1) v *= -1;
         U[at(g, r, dst, ej)] = v;
+      }
+    } else if (t >= 2 * nyg + 2 * nxg) {  // the 4 x 16 corner ghosts
+      const int c = t - 2 * nyg - 2 * nxg;
+      const int sidex = c >> 5, sidey = (c >> 4) & 1;
+      const int kx = ((c >> 2) & 3) + 1, ky = (c & 3) + 1;
+      const int ei = sidex == 0 ? sx - kx : ex - 1 + kx;
+      const int ej = sidey == 0 ? sy - ky : ey - 1 + ky;
+      const int bcx = sidex == 0 ? g.bc_left : g.bc_right;
+      const int srcy = g.bc_y == kPeriod ? (sidey == 0 ? ey - 1 - ky : sy + ky) : (sidey == 0 ? sy + ky : ey - 1 - ky);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double v;
+        if (bcx == kSpecial) {
+          v = special[8 * g.nxt + (sidex * 4 + r) * g.nyt + ej];
+        } else {
+          const int col = bcx == kPeriod ? (sidex == 0 ? ex - 1 - kx : sx + kx) : (sidex == 0 ? sx + kx : ex - 1 - kx);
+          // y rule at ghost column ei (x periodic: its interior rows hold
+          // column col) or at interior column col (x not periodic)
+          if (g.bc_y == kSpecial) v = special[(sidey * 4 + r) * g.nxt + (bcx == kPeriod ? ei : col)];
+          else v = U[at(g, r, col, srcy)];
+          if (g.bc_y == kSlip && r == 2) v *= -1;
+          if (bcx == kSlip && r == 1) v *= -1;
+        }
+        U[at(g, r, ei, ej)] = v;
       }
     } else {  // y ghosts on interior columns
       const int u = t - 2 * nyg;
@@ -290,7 +319,7 @@ Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lam
 }
 
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s) {
-  const long long work = 8LL * (g.nx + g.ny);
+  const long long work = 8LL * (g.nx + g.ny) + 64;
   k_bc_fill<<<grid_for(work, 256), 256, 0, s>>>(g, U, special, active);
   return cudaGetLastError();
 }

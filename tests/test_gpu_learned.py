@@ -78,7 +78,8 @@ def test_tensor_core_indicator_matches_fp32_forward():
     want = logits > 0.0
     # BF16 operands can flip cells whose logit is within rounding of the threshold
     close = np.abs(logits) < 0.05 * np.maximum(1.0, np.abs(logits).max())
-    assert np.array_equal(flags[~close].astype(bool), want[~close])
+    bad = np.nonzero(flags[~close].astype(bool) != want[~close])[0]
+    assert len(bad) == 0, f"{len(bad)} of {np.sum(~close)} flags differ, first cells {bad[:5]}
     assert 0.01 < want.mean() < 0.99
 
 
@@ -117,9 +118,15 @@ def test_trained_indicator_gain_over_the_method_without_it():
     discontinuities (recall) while sending most faces to the cheap flux."""
     X, y = learned.generate_dataset(torch, runs=((4, 21), (4, 22), (5, 23)), n=256, snapshots=(20, 60, 120),
                                     per_snapshot=40_000)
+    p0 = learned.init_params(0)
+    grad = torch.empty(wenofd.MLP_PARAMS, device="cuda")
+    loss0 = torch.empty(1, device="cuda")
+    dp0 = torch.from_numpy(p0).cuda()
+    wenofd.mlp_backward(dp0.data_ptr(), X.data_ptr(), y.data_ptr(), len(y), grad.data_ptr(), loss0.data_ptr())
     params, losses = learned.train(torch, X, y, epochs=12, batch=2048, lr=3e-3)
-    assert losses[-1] < 0.6 * losses[0]
-    recall, precision, _ = learned.recall_precision(torch, params, X, y, threshold=0.3)
+    recall, precision, frac = learned.recall_precision(torch, params, X, y, threshold=0.3)
+    print(f"loss {float(loss0.cpu()[0]):.4f} -> {losses[-1]:.4f}; train recall {recall:.3f} precision {precision:.3f}")
+    assert losses[-1] < 0.7 * float(loss0.cpu()[0])
     assert recall > 0.9
     n, steps, seed = 256, 80, 31
     ref, _ = _run(n, 4, seed, wenofd.FP64, steps)
