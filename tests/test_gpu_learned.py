@@ -79,7 +79,7 @@ def test_tensor_core_indicator_matches_fp32_forward():
     # BF16 operands can flip cells whose logit is within rounding of the threshold
     close = np.abs(logits) < 0.05 * np.maximum(1.0, np.abs(logits).max())
     bad = np.nonzero(flags[~close].astype(bool) != want[~close])[0]
-    assert len(bad) == 0, f"{len(bad)} of {np.sum(~close)} flags differ, first cells {bad[:5]}
+    assert len(bad) == 0, f"{len(bad)} of {np.sum(~close)} flags differ, first cells {bad[:5]}"
     assert 0.01 < want.mean() < 0.99
 
 
