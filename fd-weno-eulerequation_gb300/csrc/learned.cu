@@ -32,7 +32,7 @@ namespace lrn {
 constexpr int kIn = 50, kHid = 32;
 constexpr int oW1 = 0, oB1 = 1600, oW2 = 1632, oB2 = 2656, oW3 = 2688, oB3 = 2720;
 constexpr int kParams = 2721;
-constexpr float kFlat = 1e-2f;  // relative range below which a window counts as flat
+constexpr float kFlat = 1e-4f;  // relative range below which a window counts as flat
 
 __device__ __forceinline__ float gelu(float z) {
   const float k = 0.7978845608028654f;  // sqrt(2/pi)
@@ -51,7 +51,7 @@ __device__ __forceinline__ float pressure32(float gamma, float r, float mu, floa
 }
 
 // (v - centre) / max|v - centre| over the 25-point window, or zeros when the
-// window is flat (range <= 1e-2 (|centre| + 1e-12)).
+// window is flat (range <= 1e-4 (|centre| + 1e-12)).
 __device__ __forceinline__ void normalise(const float w[25], float out[25]) {
   const float c = w[12];
   float R = 0.0f;

@@ -148,7 +148,7 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch);
 
 /* ---- Learned troubled-cell indicator (no counterpart in the reference) ----
  * Network: 50 inputs (5x5 windows of density and pressure, each normalised
- * as (v - v_centre) / max|v - v_centre|, zero when that range is <= 1e-2 of
+ * as (v - v_centre) / max|v - v_centre|, zero when that range is <= 1e-4 of
  * |v_centre|) -> 32 -> 32 -> 1, GELU (tanh form) hidden layers, sigmoid
  * output.  Parameters are WENOFD_MLP_PARAMS floats: W1[32][50], b1[32],
  * W2[32][32], b2[32], w3[32], b3. */

@@ -781,7 +781,7 @@ static void normalise_window(const float w[25], float out[25]) {
     const float d = fabsf(w[k] - c);
     if (d > R) R = d;
   }
-  if (R <= 1e-2f * (fabsf(c) + 1e-12f)) {
+  if (R <= 1e-4f * (fabsf(c) + 1e-12f)) {
     for (int k = 0; k < 25; ++k) out[k] = 0.0f;
     return;
   }

@@ -123,7 +123,7 @@ def test_trained_indicator_gain_over_the_method_without_it():
     loss0 = torch.empty(1, device="cuda")
     dp0 = torch.from_numpy(p0).cuda()
     wenofd.mlp_backward(dp0.data_ptr(), X.data_ptr(), y.data_ptr(), len(y), grad.data_ptr(), loss0.data_ptr())
-    params, losses = learned.train(torch, X, y, epochs=12, batch=2048, lr=3e-3)
+    params, losses = learned.train(torch, X, y, epochs=20, batch=2048, lr=3e-3)
     recall, precision, frac = learned.recall_precision(torch, params, X, y, threshold=0.3)
     print(f"loss {float(loss0.cpu()[0]):.4f} -> {losses[-1]:.4f}; train recall {recall:.3f} precision {precision:.3f}")
     assert losses[-1] < 0.7 * float(loss0.cpu()[0])
@@ -141,3 +141,29 @@ def test_trained_indicator_gain_over_the_method_without_it():
     assert np.all(np.isfinite(lrn))
     print(f"flagged {f_lrn:.3f}; L1 rho vs FP64 WENO-Z: linear {e_lin:.3e}, learned {e_lrn:.3e}, "
           f"FP32 WENO {e_weno:.3e}; recall {recall:.3f} precision {precision:.3f}")
+
+
+def test_learned_error_against_finer_reference_within_bound():
+    """The accuracy bar of the learned + FP32 form: its L1 density error
+    against a 2x finer plain FP64 WENO-Z solution (node-based refinement,
+    fine node 2k = coarse node k) is at most 1.5x that of plain FP64 WENO-Z
+    at the coarse resolution, at the same end time."""
+    X, y = learned.generate_dataset(torch, runs=((4, 21), (4, 22), (5, 23)), n=256, snapshots=(20, 60, 120),
+                                    per_snapshot=40_000)
+    params, _ = learned.train(torch, X, y, epochs=20, batch=2048, lr=3e-3)
+
+    def state_at(n, prec, par=None):
+        with wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
+                            "SEED": 31, "PRECISION": prec, "TEND": 0.1}) as s:
+            s.initialize()
+            if par is not None:
+                s.set_indicator(par, 0.3)
+            s.advance(-1)
+            return s.get_state()
+
+    n = 257
+    fine = state_at(2 * n - 1, wenofd.FP64)[:, ::2, ::2]
+    e64 = np.mean(np.abs(state_at(n, wenofd.FP64)[0] - fine[0]))
+    elr = np.mean(np.abs(state_at(n, wenofd.LEARNED, params)[0] - fine[0]))
+    print(f"L1 rho vs 2x finer FP64: plain FP64 {e64:.4e}, learned+FP32 {elr:.4e} (ratio {elr / e64:.3f})")
+    assert elr <= 1.5 * e64
