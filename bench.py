@@ -7,10 +7,15 @@ step (time-step reduction + 3 stages with their boundary fills) over the
 whole grid; cell-updates = nodes x steps.  The state (537 MB per array) is
 larger than L2, so no flush is needed between steps.
 
-The headline form is the fastest form that is built (FP32 flux arithmetic
-with FP64 state / RK sums / dt); the plain FP64 WENO-Z path, bitwise equal to
-the reference, is measured in the same run on the same GPU, and the density
-L1 difference between the two after the same steps is reported.
+The headline form is learned + FP32: each step a BF16 tensor-core MLP flags
+troubled nodes, faces near them take characteristic WENO-Z and all others the
+linear fifth-order upwind flux, in FP32 arithmetic with FP64 state, RK sums
+and dt.  The indicator is trained on the GPU during setup (untimed) on
+solver-produced stencils at other seeds.  The FP32 form (WENO-Z everywhere)
+and the plain FP64 WENO-Z path, bitwise equal to the reference, are measured
+in the same run on the same GPU.  L1 density errors are reported against the
+plain FP64 path on the same grid after the same steps, and against a 2x finer
+plain FP64 solution at 513^2 (the accuracy bar: <= 1.5x plain FP64's error).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -35,6 +40,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 N = 4096
 SEED = 2024
+THRESHOLD = 0.3  # indicator probability above which a node is flagged
 METRIC = "cell-updates/s at 4096^2 (learned+FP32 vs plain FP64 WENO-Z, same GB300) at stated L1 err"
 # algorithmic HBM bytes per node for one SSP-RK3 step with FP64 state:
 # stage 1 reads U^n, writes U1 (64 B); stages 2, 3 read U^n and U^k, write (96 B each)
@@ -155,10 +161,12 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line))
 
 
-def time_form(wenofd, torch, precision: int, device: int, steps: int, warmup: int, stream):
+def time_form(wenofd, torch, precision: int, device: int, steps: int, warmup: int, stream, params=None):
     s = wenofd.Solver(config_for(precision, device))
     s.set_stream(stream.cuda_stream)
     s.initialize()
+    if params is not None:
+        s.set_indicator(params, THRESHOLD)
     s.advance(max_steps=warmup)
     l0 = s.info().launches
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -173,6 +181,49 @@ def time_form(wenofd, torch, precision: int, device: int, steps: int, warmup: in
     return s, ms, launches
 
 
+def train_indicator(torch, device: int):
+    """The indicator is trained on the GPU before timing: solver-produced
+    stencils (two shear layers, two Riemann problems, seeds != SEED, 512^2,
+    2e6 samples) and the project's FP32 training kernels."""
+    from wenofd import learned
+
+    t0 = time.perf_counter()
+    X, y = learned.generate_dataset(torch, device=device)
+    t1 = time.perf_counter()
+    params, losses = learned.train(torch, X, y, epochs=30, batch=4096, lr=3e-3)
+    t2 = time.perf_counter()
+    recall, precision, _ = learned.recall_precision(torch, params, X[:200000], y[:200000], THRESHOLD)
+    info = {"samples": int(len(y)), "positive_fraction": float(y.mean()), "epochs": 30,
+            "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
+            "recall": recall, "precision": precision, "threshold": THRESHOLD,
+            "data_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2)}
+    del X, y
+    return params, info
+
+
+def finer_reference_errors(wenofd, params, device: int, n: int = 513, t_end: float = 0.1) -> dict:
+    """L1 density error of each form at n^2 against plain FP64 WENO-Z on the
+    2x finer node grid (2n-1)^2 at the same end time (fine node 2k = coarse
+    node k), shear layer, seed SEED."""
+    def state_at(m, prec, par=None):
+        cfg = dict(config_for(prec, device), ELEMNUMX=m, ELEMNUMY=m, TEND=t_end)
+        with wenofd.Solver(cfg) as s:
+            s.initialize()
+            if par is not None:
+                s.set_indicator(par, THRESHOLD)
+            s.advance(-1)
+            return s.get_state()[0]
+    import numpy as np
+
+    fine = state_at(2 * n - 1, wenofd.FP64)[::2, ::2]
+    e = {name: float(np.mean(np.abs(state_at(n, prec, par) - fine)))
+         for name, prec, par in (("fp64", wenofd.FP64, None), ("fp32", wenofd.FP32, None),
+                                 ("learned_fp32", wenofd.LEARNED, params))}
+    e["ratio_learned_to_fp64"] = e["learned_fp32"] / e["fp64"]
+    e["setup"] = f"shear layer {n}^2 vs {2 * n - 1}^2 plain FP64 WENO-Z, t = {t_end}"
+    return e
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,8 +232,9 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-errors", action="store_true", help="skip the 2x finer reference run")
     ap.add_argument("--only-headline", action="store_true",
-                    help="time the headline form only (no FP64 leg, error, e2e or CPU leg): for profiling")
+                    help="time the headline form only (no other legs, errors, e2e or CPU leg): for profiling")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -218,19 +270,28 @@ def main() -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # ---- headline form (FP32 flux arithmetic), device-timed
+    params, train_info = train_indicator(torch, local)
+
+    # ---- headline: learned indicator + FP32 flux arithmetic, device-timed
     barrier()
     with ClockSampler(local) as clk:
-        s32, ms32, launches = time_form(wenofd, torch, wenofd.FP32, local, args.steps, args.warmup, stream)
-    ms32 = max_over_ranks(ms32)
-    value = world * args.steps * cells / (ms32 / 1e3)
+        sl, msl, launches = time_form(wenofd, torch, wenofd.LEARNED, local, args.steps, args.warmup, stream, params)
+    msl = max_over_ranks(msl)
+    value = world * args.steps * cells / (msl / 1e3)
+    flagged = float(sl.indicator_flags().mean())
     if args.only_headline:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "steps": args.steps,
-                              "ms_per_step": ms32 / args.steps, "gpu_launches": launches,
+                              "ms_per_step": msl / args.steps, "gpu_launches": launches, "flagged": flagged,
                               "note": "headline form only (profiling run)"}))
-        s32.close()
+        sl.close()
         return
+
+    # ---- FP32 form (every face characteristic WENO-Z)
+    barrier()
+    s32, ms32, _ = time_form(wenofd, torch, wenofd.FP32, local, args.steps, args.warmup, stream)
+    ms32 = max_over_ranks(ms32)
+    value32 = world * args.steps * cells / (ms32 / 1e3)
 
     # ---- plain FP64 WENO-Z (bitwise the reference) on the same GPU
     k64 = args.fp64_steps if args.fp64_steps is not None else max(2, min(args.steps, 5))
@@ -238,44 +299,48 @@ def main() -> None:
     s64, ms64, _ = time_form(wenofd, torch, wenofd.FP64, local, k64, args.warmup, stream)
     ms64 = max_over_ranks(ms64)
     value64 = world * k64 * cells / (ms64 / 1e3)
+    s64.close()
 
-    # density difference after the same number of steps from the same state
-    rho32 = s32.get_state()[0]
+    # ---- same-grid density differences after the same steps from the same state
     s64b = wenofd.Solver(config_for(wenofd.FP64, local))
     s64b.set_stream(stream.cuda_stream)
     s64b.initialize()
     s64b.advance(max_steps=args.warmup + args.steps)
     rho64 = s64b.get_state()[0]
-    l1 = float(np.mean(np.abs(rho32 - rho64)))
-    linf = float(np.max(np.abs(rho32 - rho64)))
     s64b.close()
-    s64.close()
+    same_grid = {}
+    for name, sv in (("learned_fp32", sl), ("fp32", s32)):
+        d = sv.get_state()[0] - rho64
+        same_grid[name] = {"l1": float(np.mean(np.abs(d))), "linf": float(np.max(np.abs(d)))}
+    ref_err = None if args.no_reference_errors else finer_reference_errors(wenofd, params, local)
 
-    # ---- stage kernel alone (roofline): mean launch duration, CUDA events on its stream
-    ms_stage = s32.time_stages(reps=3)
+    # ---- stage kernels alone (roofline): mean launch duration, CUDA events on their stream
+    ms_stage = sl.time_stages(reps=3)
+    ms_stage32 = s32.time_stages(reps=3)
+    s32.close()
     bytes_per_launch = BYTES_PER_CELL_RK3 / 3.0 * cells
     achieved = bytes_per_launch / (ms_stage / 1e3) / 1e9
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
-    traffic = committed_traffic().get("stage_fp32_wenoz_4096", {}).get("dram_bytes_per_launch")
+    traffic = committed_traffic().get("stage_learned_wenoz_4096", {}).get("dram_bytes_per_launch")
 
     # ---- end to end through the C ABI with pinned host buffers
     host = torch.empty((4, N, N), dtype=torch.float64, pin_memory=True)
-    s32.initialize()
-    s32.get_state_ptr(host.data_ptr())
-    s32.advance(max_steps=1)
+    sl.initialize()
+    sl.get_state_ptr(host.data_ptr())
+    sl.advance(max_steps=1)
     k_e2e = max(3, min(args.steps, 10))
     barrier()
     torch.cuda.synchronize(local)
     t0 = time.perf_counter()
     for _ in range(k_e2e):
-        s32.set_state_ptr(host.data_ptr())
-        s32.advance(max_steps=1)
-        s32.get_state_ptr(host.data_ptr())
+        sl.set_state_ptr(host.data_ptr())
+        sl.advance(max_steps=1)
+        sl.get_state_ptr(host.data_ptr())
     torch.cuda.synchronize(local)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * k_e2e * cells / e2e_s
-    s32.close()
+    sl.close()
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -285,24 +350,26 @@ def main() -> None:
         clocks = clk.summary()
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32 / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": msl / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": f"shear layer {N}x{N}, SSP-RK3, WENO-Z, CFL 0.7, seed {SEED}",
-                       "form": "FP32 flux/reconstruction, FP64 state, RK sums and dt",
+                       "form": "learned troubled-cell indicator (BF16 tensor-core MLP) routing faces to linear "
+                               "upwind or characteristic WENO-Z; FP32 flux arithmetic; FP64 state, RK sums, dt",
                        "l2": "inputs larger than L2 (537 MB per state array)",
                        "parallelism": f"replicas x{world}"},
+            "flagged_fraction": flagged,
+            "indicator_training": train_info,
+            "fp32_form": {"value": value32, "unit": "cell-updates/s", "ms_per_step": ms32 / args.steps},
             "plain_fp64": {"value": value64, "unit": "cell-updates/s", "steps": k64,
                            "ms_per_step": ms64 / k64, "dtype": "f64", "parity": "bitwise vs reference"},
             "speedup_vs_plain_fp64": value / value64,
-            "l1_rho_vs_fp64": l1, "linf_rho_vs_fp64": linf,
-            "err_note": f"FP32 form vs plain FP64 GPU path (= FP64 oracle bitwise) after "
-                        f"{args.warmup + args.steps} steps from the same state",
+            "l1_err": {"same_grid_vs_fp64_after_steps": same_grid, "vs_2x_finer_fp64": ref_err},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_stage<float, WENO-Z> (one RK stage)",
-                         "ms_per_launch": ms_stage,
+                         "kernel": "k_stage<float, WENO-Z, routed> (one RK stage)",
+                         "ms_per_launch": ms_stage, "fp32_form_ms_per_launch": ms_stage32,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks
                          else "fallback 6800 GB/s"},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "steps": k_e2e,
