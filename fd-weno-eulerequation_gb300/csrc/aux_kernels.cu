@@ -1,6 +1,7 @@
 // Boundary fill, time-step reduction, time-loop control and FP64 norm
 // kernels.  Compiled with -fmad=false like the FP64 stage: the time step is
 // part of the parity contract.
+#include "convert.cuh"
 #include "wenofd_internal.h"
 
 #include <math.h>
@@ -151,10 +152,120 @@ __global__ void k_dt_reduce(Geom g, const double *U, Ctrl *c) {
   }
 }
 
+// One node's s = lx/dx + ly/dy exactly as calculateDeltaT forms it
+// (src/WENOFD.cpp:419-423 with utils/equations.hpp:137-147).
+__device__ __forceinline__ double exact_speed(const Geom &g, double rho, double mu, double mv, double E) {
+  const double gamma = g.gamma;
+  const double u = mu / rho, v = mv / rho;
+  const double p = (gamma - 1.0) * (E - 0.5 * rho * (u * u + v * v));
+  const double cs = sqrt(gamma * p / rho);
+  const double lx = fabs(u * 1.0 + v * 0.0) + cs;
+  const double ly = fabs(u * 0.0 + v * 1.0) + cs;
+  return lx / g.dx + ly / g.dy;
+}
+
+// FP32 estimate s32 of a node's s and a bound e with |s32 - s| <= e.  Error
+// budget (eps = 2^-23): inputs truncated to FP32 (eps each), u and v from
+// __fdividef (3 eps), kinetic energy ke (< 9.5 eps relative), so
+// p = (gamma-1)(E - ke) carries at most 12 eps (|E| + ke) / (E - ke)
+// relative error (the cancellation term); c = sqrt(gamma p / rho) half of
+// that plus 2 eps; the final bound takes 4x the propagated sum.  Nodes with
+// a non-positive or non-finite FP32 pressure get e = inf.
+__device__ __forceinline__ void screen_speed(const Geom &g, double rho_d, double mu_d, double mv_d, double E_d,
+                                             float &s, float &e) {
+  const float eps = 1.1920929e-07f;
+  const float r = dev::f64_to_f32(rho_d), mu = dev::f64_to_f32(mu_d), mv = dev::f64_to_f32(mv_d),
+              E = dev::f64_to_f32(E_d);
+  const float u = __fdividef(mu, r), v = __fdividef(mv, r);
+  const float ke = 0.5f * r * (u * u + v * v);
+  const float pp = E - ke;
+  const float c2 = __fdividef(g.gamma32 * ((g.gamma32 - 1.0f) * pp), r);
+  if (!(pp > 0.0f) || !(c2 > 0.0f) || !(c2 < 3.0e38f) || !(fabsf(u) < 3.0e38f) || !(fabsf(v) < 3.0e38f)) {
+    s = 0.0f;
+    e = __int_as_float(0x7f800000);
+    return;
+  }
+  const float c = sqrtf(c2);
+  const float au = fabsf(u), av = fabsf(v);
+  s = (au + c) * g.inv_dx32 + (av + c) * g.inv_dy32;
+  const float rp = 12.0f * eps * (fabsf(E) + ke) / pp;
+  const float rc = 0.5f * rp + 2.0f * eps;
+  const float ex = au * 3.0f * eps + c * rc, ey = av * 3.0f * eps + c * rc;
+  e = 4.0f * ((ex * g.inv_dx32 + ey * g.inv_dy32) + s * 4.0f * eps) + 1e-12f * s;
+}
+
+// Pass 1: L = max over nodes of (s32 - e), a lower bound of max s.
+__global__ void k_dt_screen(Geom g, const double *U, Ctrl *c) {
+  if (!c->active) return;
+  const long long n = (long long)g.nx * g.ny;
+  float lo = 0.0f;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+    const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    float s, e;
+    screen_speed(g, U[b], U[g.plane + b], U[2 * g.plane + b], U[3 * g.plane + b], s, e);
+    lo = fmaxf(lo, s - e);
+  }
+  for (int o = 16; o > 0; o >>= 1) lo = fmaxf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+  __shared__ float wl[32];
+  if ((threadIdx.x & 31) == 0) wl[threadIdx.x >> 5] = lo;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, wl[w]);
+    atomicMax(&c->screen_bits, __float_as_uint(m));
+  }
+}
+
+// Pass 2: the exact FP64 s of every node with s32 + e >= L (the node holding
+// the maximum is one of them), max-reduced as in k_dt_reduce.
+__global__ void k_dt_refine(Geom g, const double *U, Ctrl *c) {
+  if (!c->active) return;
+  const float L = __uint_as_float(c->screen_bits);
+  const long long n = (long long)g.nx * g.ny;
+  double smax = 0.0;
+  int nan_seen = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+    const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const double rho = U[b], mu = U[g.plane + b], mv = U[2 * g.plane + b], E = U[3 * g.plane + b];
+    float s32, e;
+    screen_speed(g, rho, mu, mv, E, s32, e);
+    if (s32 + e >= L) {
+      const double s = exact_speed(g, rho, mu, mv, E);
+      if (s != s) nan_seen = 1;
+      else if (s > smax) smax = s;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double other = __shfl_xor_sync(0xffffffffu, smax, o);
+    smax = other > smax ? other : smax;
+    nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
+  }
+  __shared__ double wmax[32];
+  __shared__ int wnan[32];
+  if ((threadIdx.x & 31) == 0) {
+    wmax[threadIdx.x >> 5] = smax;
+    wnan[threadIdx.x >> 5] = nan_seen;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    int nn = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      m = wmax[w] > m ? wmax[w] : m;
+      nn |= wnan[w];
+    }
+    atomicMax(&c->max_s_bits, (unsigned long long)__double_as_longlong(m));
+    if (nn) atomicOr(&c->nan_flag, 1);
+  }
+}
+
 // Open the gate for one host-driven operation (calc_dt, rk_step, step).
 __global__ void k_ctrl_open(Ctrl *c) {
   c->active = 1;
   c->max_s_bits = 0ull;
+  c->screen_bits = 0u;
   c->nan_flag = 0;
   c->error = 0;
 }
@@ -172,6 +283,7 @@ __global__ void k_dt_finalize(Ctrl *c) {
   if (!c->active) return;
   const double ms = __longlong_as_double((long long)c->max_s_bits);
   c->max_s_bits = 0ull;
+  c->screen_bits = 0u;
   if (c->nan_flag) {
     c->nan_flag = 0;
     c->error = 3;  // WENOFD_NAN_DT
@@ -213,6 +325,7 @@ __global__ void k_advance_setup(Ctrl *c, long long max_steps) {
   c->max_steps = max_steps < 0 ? 0x7fffffffffffffffLL : c->steps + max_steps;
   c->done = !(fabs(c->now - c->t_end) > 1e-9);
   c->max_s_bits = 0ull;
+  c->screen_bits = 0u;
   c->nan_flag = 0;
 }
 
@@ -315,6 +428,10 @@ Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lam
   g.bc_right = bc_right;
   g.bc_y = bc_y;
   g.gravity = gravity;
+  g.gamma32 = float(gamma);
+  g.zpl32 = float(zp_lambda);
+  g.inv_dx32 = float(1.0 / dx);
+  g.inv_dy32 = float(1.0 / dy);
   return g;
 }
 
@@ -326,6 +443,13 @@ cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, cons
 
 cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream_t s) {
   k_dt_reduce<<<grid_for((long long)g.nx * g.ny, 256), 256, 0, s>>>(g, U, c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, cudaStream_t s) {
+  const int grid = grid_for((long long)g.nx * g.ny, 256);
+  k_dt_screen<<<grid, 256, 0, s>>>(g, U, c);
+  k_dt_refine<<<grid, 256, 0, s>>>(g, U, c);
   return cudaGetLastError();
 }
 

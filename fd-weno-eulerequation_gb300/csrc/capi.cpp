@@ -182,15 +182,28 @@ int enqueue_rk(wenofd_solver *s) {
   return fail(WENOFD_BAD_CONFIG, "Error: Invalid Runge-Kutta method");
 }
 
+// The time-step reduction: FP64 form one FP64 pass; FP32 forms the two-pass
+// reduction (same result bit for bit, FP32 screen + FP64 refine).
+int enqueue_dt_reduce(wenofd_solver *s) {
+  if (s->precision == WENOFD_FP64) {
+    CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+    s->launches += 1;
+  } else {
+    CUDA_TRY(wenofd::launch_dt_reduce_two_pass(s->g, s->S, s->ctrl, s->stream));
+    s->launches += 2;
+  }
+  return WENOFD_OK;
+}
+
 // One graph-driven step: gate, dt reduction, dt, stages, time update.
 int enqueue_step(wenofd_solver *s) {
   CUDA_TRY(wenofd::launch_step_begin(s->ctrl, s->stream));
-  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
   int rc = enqueue_rk(s);
   if (rc) return rc;
   CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
-  s->launches += 4;
+  s->launches += 3;
   return WENOFD_OK;
 }
 
@@ -544,9 +557,9 @@ int wenofd_calc_dt(wenofd_solver *s, double *dt) {
   if (!dt) return fail(WENOFD_BAD_ARG, "null dt");
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
-  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
-  s->launches += 3;
+  s->launches += 2;
   if (int rc = read_ctrl(s)) return rc;
   if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
   *dt = s->ctrl_host->dt;
@@ -565,11 +578,11 @@ int wenofd_step(wenofd_solver *s, double *dt_out) {
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
-  CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
+  if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
   if (int rc = enqueue_rk(s)) return rc;
   CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
-  s->launches += 4;
+  s->launches += 3;
   if (int rc = read_ctrl(s)) return rc;
   if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
   if (dt_out) *dt_out = s->ctrl_host->dt;

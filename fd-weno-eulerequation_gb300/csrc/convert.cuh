@@ -1,0 +1,53 @@
+// FP64 <-> FP32 conversions on the integer ALU.
+//
+// On GB300 the conversion instructions between FP64 and FP32 issue on the
+// FP64 pipe, which runs at 1/64 of the FP32 rate (1.0 vs 73 TFLOP/s
+// measured); the FP32 form converts every staged state value and every RHS
+// value, so it does the conversions with bit operations instead.
+//
+//  f64_to_f32: rounds toward zero (error < 1 FP32 ulp); magnitudes below
+//              2^-126 become signed zero, above the FP32 range infinity; NaN
+//              stays NaN.  Used only where the FP32 form reads the state.
+//  f32_to_f64: exact for every finite float (FP32 subnormals become zero),
+//              infinity and NaN preserved.
+#pragma once
+
+namespace wenofd {
+namespace dev {
+
+__device__ __forceinline__ float f64_to_f32(double d) {
+  const unsigned hi = unsigned(__double2hiint(d));
+  const unsigned lo = unsigned(__double2loint(d));
+  const unsigned sign = hi & 0x80000000u;
+  const int e = int((hi >> 20) & 0x7ffu);  // double exponent field
+  const int e32 = e - 896;                  // 1023 - 127
+  const unsigned mant = ((hi & 0x000fffffu) << 3) | (lo >> 29);
+  unsigned bits;
+  if (e32 <= 0) bits = sign;                                             // zero, subnormal, tiny
+  else if (e == 0x7ff) bits = sign | 0x7f800000u | (((hi & 0x000fffffu) | lo) ? 0x400000u : 0u);  // inf / NaN
+  else if (e32 >= 255) bits = sign | 0x7f800000u;                        // beyond FP32 range
+  else bits = sign | (unsigned(e32) << 23) | mant;
+  return __uint_as_float(bits);
+}
+
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned sign = b & 0x80000000u;
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned m = b & 0x7fffffu;
+  unsigned hi, lo;
+  if (e == 0) {  // zero (FP32 subnormals flush to zero)
+    hi = sign;
+    lo = 0;
+  } else if (e == 0xffu) {
+    hi = sign | 0x7ff00000u | (m >> 3);
+    lo = m << 29;
+  } else {
+    hi = sign | ((e + 896u) << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double(int(hi), int(lo));
+}
+
+}  // namespace dev
+}  // namespace wenofd

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/wenofd.h"
+#include "convert.cuh"
 #include "physics.cuh"
 #include "wenofd_internal.h"
 
@@ -50,7 +51,7 @@ __device__ __forceinline__ float pressure32(float gamma, float r, float mu, floa
   return (gamma - 1.0f) * (E - 0.5f * r * (u * u + v * v));
 }
 
-// (v - centre) / max|v - centre| over the 25-point window, or zeros when the
+// (v - centre) * (1 / max|v - centre|) over the 25-point window, or zeros when the
 // window is flat (range <= 1e-4 (|centre| + 1e-12)).
 __device__ __forceinline__ void normalise(const float w[25], float out[25]) {
   const float c = w[12];
@@ -62,8 +63,17 @@ __device__ __forceinline__ void normalise(const float w[25], float out[25]) {
     for (int k = 0; k < 25; ++k) out[k] = 0.0f;
     return;
   }
+  const float inv = 1.0f / R;
 #pragma unroll
-  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) / R;
+  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) * inv;
+}
+
+// GELU for inference: the same tanh form with the hardware tanh
+// approximation (the BF16 operands that follow are coarser than its error).
+__device__ __forceinline__ float gelu_fast(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.7978845608028654f * (z + 0.044715f * z * z * z)));
+  return 0.5f * z * (1.0f + t);
 }
 
 // ------------------------------------------------------------- features
@@ -440,8 +450,9 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
       float r = 1.0f, p = 1.0f;
       if (ei < g.nxt && ej < g.nyt) {
         const long long b = (long long)ei * g.pitch + ej;
-        r = float(U[b]);
-        p = pressure32(gam, r, float(U[g.plane + b]), float(U[2 * g.plane + b]), float(U[3 * g.plane + b]));
+        r = dev::f64_to_f32(U[b]);
+        p = pressure32(gam, r, dev::f64_to_f32(U[g.plane + b]), dev::f64_to_f32(U[2 * g.plane + b]),
+                       dev::f64_to_f32(U[3 * g.plane + b]));
       }
       sRho[k] = r;
       sPre[k] = p;
@@ -450,20 +461,33 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
     // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1
     {
       const int ci = warp, cj = tid & 31;
-      float w[25], o[25];
-      __align__(16) __nv_bfloat16 row[kK1];
-      for (int a = 0; a < 5; ++a)
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[(ci + a) * kPJ + cj + b];
-      normalise(w, o);
-      for (int k = 0; k < 25; ++k) row[k] = __float2bfloat16_rn(o[k]);
-      for (int a = 0; a < 5; ++a)
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[(ci + a) * kPJ + cj + b];
-      normalise(w, o);
-      for (int k = 0; k < 25; ++k) row[25 + k] = __float2bfloat16_rn(o[k]);
-      for (int k = 50; k < kK1; ++k) row[k] = __float2bfloat16_rn(0.0f);
+      float f[kK1];
+      float w[25];
 #pragma unroll
-      for (int c = 0; c < kK1 / 8; ++c)
-        *reinterpret_cast<uint4 *>(&sA1[canon_off(tid, 8 * c, kK1 / 8)]) = *reinterpret_cast<const uint4 *>(&row[8 * c]);
+      for (int a = 0; a < 5; ++a)
+#pragma unroll
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[(ci + a) * kPJ + cj + b];
+      normalise(w, f);
+#pragma unroll
+      for (int a = 0; a < 5; ++a)
+#pragma unroll
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[(ci + a) * kPJ + cj + b];
+      normalise(w, f + 25);
+#pragma unroll
+      for (int k = 50; k < kK1; ++k) f[k] = 0.0f;
+#pragma unroll
+      for (int c = 0; c < kK1 / 8; ++c) {
+        uint4 q;
+        __nv_bfloat162 h0 = __floats2bfloat162_rn(f[8 * c + 0], f[8 * c + 1]);
+        __nv_bfloat162 h1 = __floats2bfloat162_rn(f[8 * c + 2], f[8 * c + 3]);
+        __nv_bfloat162 h2 = __floats2bfloat162_rn(f[8 * c + 4], f[8 * c + 5]);
+        __nv_bfloat162 h3 = __floats2bfloat162_rn(f[8 * c + 6], f[8 * c + 7]);
+        q.x = *reinterpret_cast<unsigned *>(&h0);
+        q.y = *reinterpret_cast<unsigned *>(&h1);
+        q.z = *reinterpret_cast<unsigned *>(&h2);
+        q.w = *reinterpret_cast<unsigned *>(&h3);
+        *reinterpret_cast<uint4 *>(&sA1[canon_off(tid, 8 * c, kK1 / 8)]) = q;
+      }
     }
     fence_async_smem();
     tc_fence_before();
@@ -488,12 +512,18 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
     {
       float z[32];
       tmem_ld32(tmem + lane_base, z);
-      __align__(16) __nv_bfloat16 row[kK2];
 #pragma unroll
-      for (int o = 0; o < kHid; ++o) row[o] = __float2bfloat16_rn(gelu(z[o] + sb1[o]));
+      for (int c = 0; c < kK2 / 8; ++c) {
+        uint4 q;
+        unsigned *qq = reinterpret_cast<unsigned *>(&q);
 #pragma unroll
-      for (int c = 0; c < kK2 / 8; ++c)
-        *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 8 * c, kK2 / 8)]) = *reinterpret_cast<const uint4 *>(&row[8 * c]);
+        for (int h = 0; h < 4; ++h) {
+          const int o = 8 * c + 2 * h;
+          __nv_bfloat162 v = __floats2bfloat162_rn(gelu_fast(z[o] + sb1[o]), gelu_fast(z[o + 1] + sb1[o + 1]));
+          qq[h] = *reinterpret_cast<unsigned *>(&v);
+        }
+        *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 8 * c, kK2 / 8)]) = q;
+      }
     }
     fence_async_smem();
     tc_fence_before();
@@ -521,7 +551,7 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
       tmem_ld32(tmem + lane_base + 32, z);
       float logit = sb3;
 #pragma unroll
-      for (int o = 0; o < kHid; ++o) logit += sw3[o] * gelu(z[o] + sb2[o]);
+      for (int o = 0; o < kHid; ++o) logit += sw3[o] * gelu_fast(z[o] + sb2[o]);
       const int i = i0 + warp, j = j0 + (tid & 31);
       if (i < g.nx && j < g.ny && !abort_sh)
         flags[(long long)(kGhost + i) * flag_pitch + (kGhost + j)] = logit > logit_threshold ? 1 : 0;

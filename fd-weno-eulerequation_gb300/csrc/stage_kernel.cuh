@@ -17,6 +17,7 @@
 // the y sweep.
 #pragma once
 
+#include "convert.cuh"
 #include "physics.cuh"
 
 namespace wenofd {
@@ -62,8 +63,9 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
 
   const int i0 = blockIdx.y * TI;  // first interior node of the tile (0-based)
   const int j0 = blockIdx.x * TJ;
-  const T gamma = T(g.gamma);
-  const T zpl = T(g.zp_lambda);
+  constexpr bool F32 = sizeof(T) == 4;
+  const T gamma = F32 ? T(g.gamma32) : T(g.gamma);
+  const T zpl = F32 ? T(g.zpl32) : T(g.zp_lambda);
 
   // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj
   for (int t = threadIdx.x; t < 4 * HI * HJ; t += NT) {
@@ -72,7 +74,11 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     const int hi = rem / HJ, hj = rem - hi * HJ;
     const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
     T val = T(0);
-    if (ei < g.nxt && ej < g.nyt) val = T(a.uin[r * g.plane + (long long)ei * g.pitch + ej]);
+    if (ei < g.nxt && ej < g.nyt) {
+      const double d = a.uin[r * g.plane + (long long)ei * g.pitch + ej];
+      if constexpr (F32) val = f64_to_f32(d);  // integer ALU, not the FP64 pipe
+      else val = d;
+    }
     Us[t] = val;
   }
   if constexpr (ROUTE) {
@@ -147,6 +153,7 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   constexpr int PPT = (TI * TJ + NT - 1) / NT;
   T rhs[PPT][4];
   const T dx = T(g.dx), dy = T(g.dy);
+  const T idx = T(g.inv_dx32), idy = T(g.inv_dy32);
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -155,7 +162,8 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     for (int r = 0; r < 4; ++r) {
       if (t < TI * TJ) {
         const T hr = Hf[(r * (TI + 1) + i + 1) * TJ + j], hl = Hf[(r * (TI + 1) + i) * TJ + j];
-        rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
+        if constexpr (F32) rhs[k][r] = -(hr - hl) * idx;
+        else rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
       }
     }
   }
@@ -223,6 +231,8 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
 
   // --- y term, source, RK combination, store
   const double dt = *a.dt;
+  [[maybe_unused]] const double cdt = a.c * dt;
+  [[maybe_unused]] const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -233,7 +243,8 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const T hr = Hf[(r * TI + i) * (TJ + 1) + j + 1], hl = Hf[(r * TI + i) * (TJ + 1) + j];
-      rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
+      if constexpr (F32) rr[r] = rhs[k][r] - (hr - hl) * idy;
+      else rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
     }
     const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
@@ -243,12 +254,20 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const long long idx = r * g.plane + gidx;
-      if (a.mode == kModeRHS) {
-        a.uout[idx] = double(rr[r]);
+      const long long ix = r * g.plane + gidx;
+      if constexpr (F32) {
+        // FP64 RK combination; stage 1 (a = 1, b = 0, un == uin) is one FMA
+        const double rd = f32_to_f64(rr[r]);
+        if (a.mode == kModeRHS) a.uout[ix] = rd;
+        else if (stage1) a.uout[ix] = fma(cdt, rd, a.un[ix]);
+        else a.uout[ix] = fma(cdt, rd, fma(a.b, a.uin[ix], a.a * a.un[ix]));
       } else {
-        const double un = a.un[idx], ui = a.uin[idx];
-        a.uout[idx] = a.a * un + a.b * ui + a.c * dt * double(rr[r]);
+        if (a.mode == kModeRHS) {
+          a.uout[ix] = double(rr[r]);
+        } else {
+          const double un = a.un[ix], ui = a.uin[ix];
+          a.uout[ix] = a.a * un + a.b * ui + a.c * dt * double(rr[r]);
+        }
       }
     }
   }

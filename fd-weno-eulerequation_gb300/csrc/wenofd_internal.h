@@ -28,6 +28,8 @@ struct Geom {
   double zp_lambda;  // pow(dx, 2/3), WENO-ZP (include/Utility.hpp:531; dx also in y, src/WENOFD.cpp:836)
   int bc_left, bc_right, bc_y;  // y uses the bottom condition on both sides (src/WENOFD.cpp:1009)
   int gravity;                  // RTI source term (src/WENOFD.cpp:800-821)
+  // FP32-form constants, rounded once on the host: gamma, zp_lambda, 1/dx, 1/dy
+  float gamma32, zpl32, inv_dx32, inv_dy32;
 };
 
 // Device-resident control block of the time loop.  All fields are written
@@ -35,6 +37,7 @@ struct Geom {
 struct Ctrl {
   double now, t_end, cfl, dt;
   unsigned long long max_s_bits;  // max over nodes of lx/dx + ly/dy, as IEEE bits (all >= 0)
+  unsigned screen_bits;           // FP32 lower bound of that max (two-pass reduction), as bits
   long long steps, max_steps;
   int active;    // this step runs (set per step)
   int done;      // |now - t_end| <= 1e-9 (src/WENOFD.cpp:213)
@@ -79,6 +82,10 @@ cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights
 // aux_kernels.cu
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s);
 cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream_t s);
+// Same result, bit for bit, in two passes that keep the FP64 pipe nearly
+// idle: an FP32 screen with a rigorous error bound, then FP64 only where a
+// node can hold the maximum.
+cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, cudaStream_t s);
 cudaError_t launch_ctrl_open(Ctrl *c, cudaStream_t s);
 cudaError_t launch_step_begin(Ctrl *c, cudaStream_t s);
 cudaError_t launch_dt_finalize(Ctrl *c, cudaStream_t s);

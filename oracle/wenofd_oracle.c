@@ -785,7 +785,8 @@ static void normalise_window(const float w[25], float out[25]) {
     for (int k = 0; k < 25; ++k) out[k] = 0.0f;
     return;
   }
-  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) / R;
+  const float inv = 1.0f / R;
+  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) * inv;
 }
 
 void orc_cell_features(const orc_grid *g, const double *U, float *features) {

@@ -92,7 +92,7 @@ void orc_conservation_sums(const orc_grid *g, const double *U, double out[4]);
 /* Learned troubled-cell indicator (no reference counterpart; these restate
  * this project's own definitions, for checking the CUDA kernels):
  *  features: per interior cell, the 5x5 windows of density and pressure,
- *    each normalised as (v - v_centre) / max|v - v_centre| (all zero when
+ *    each normalised as (v - v_centre) * (1 / max|v - v_centre|) (all zero when
  *    that range is <= 1e-4 (|v_centre| + 1e-12)); 50 floats, density first,
  *    window row-major in (ei, ej).  Computed in FP32 from the FP32-rounded
  *    state.  U must have its ghosts filled.

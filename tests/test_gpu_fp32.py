@@ -68,3 +68,23 @@ def test_fp32_shear_layer_stays_finite_and_close(scheme):
     rho32, rho64 = out[wenofd.FP32][0], out[wenofd.FP64][0]
     assert np.mean(np.abs(rho32 - rho64)) <= 1e-5
     assert np.max(np.abs(rho32 - rho64)) <= 1e-3
+
+
+@pytest.mark.parametrize("tc,n,steps", [(orc.RIEMANN_SEEDED, 300, 0), (orc.RIEMANN_SEEDED, 300, 15),
+                                        (orc.SHEAR, 256, 5), (orc.SMOOTH, 120, 3), (orc.RTI, 64, 5),
+                                        (orc.RIEMANN1, 200, 10)])
+def test_two_pass_time_step_equals_fp64_reduction(tc, n, steps):
+    """The FP32 forms reduce the time step in two passes (FP32 screen with an
+    error bound, FP64 only where a node can hold the maximum); the result
+    must equal the FP64 form's single FP64 pass bit for bit.  Constant
+    quadrants (step 0) make whole regions tie for the maximum."""
+    p = orc.Problem(tc, n, n, orc.WENOZ, 2, 0.7, seed=19)
+    p.run(max_steps=steps)
+    U = p.interior()
+    dts = []
+    for prec in (wenofd.FP64, wenofd.FP32, wenofd.LEARNED):
+        with wenofd.Solver({"TESTCASE": tc, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7,
+                            "SCHEME": 1, "SEED": 19, "PRECISION": prec}) as s:
+            s.set_state(U)
+            dts.append(s.calc_dt())
+    assert dts[0] == dts[1] == dts[2] == p.calc_dt()
