@@ -29,8 +29,18 @@ struct StageSmem {
   static constexpr int kU = 4 * HI * HJ;                                    // state + halo
   static constexpr int kSplit = 4 * (HI * TJ > TI * HJ ? HI * TJ : TI * HJ);  // one of F+, F-
   static constexpr int kFace = 4 * ((TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1));
-  static constexpr size_t bytes = sizeof(T) * (size_t(kU) + 2 * kSplit + kFace);
+  // FP32 form: the tile's FP64 input values (kept from the halo load) and
+  // its FP64 U^n values (prefetched with cp.async) for the RK combination.
+  static constexpr int kKeep = sizeof(T) == 4 ? 2 * 4 * TI * TJ : 0;
+  static constexpr size_t bytes = sizeof(T) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
 };
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Linear fifth-order upwind flux of one component: WENO with its weights
 // frozen at (0.1, 0.6, 0.3), on F+ at nodes face-3..face+1 (a..e) and on F-
@@ -53,6 +63,8 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   T *Fp = Us + S::kU;
   T *Fm = Fp + S::kSplit;
   T *Hf = Fm + S::kSplit;
+  double *Uin64 = reinterpret_cast<double *>(smem_raw + sizeof(T) * (size_t(S::kU) + 2 * S::kSplit + S::kFace));
+  double *Un64 = Uin64 + 4 * TI * TJ;
   // routed form: node flags of the tile with a 2-node halo, and the list of
   // faces that need WENO
   constexpr int FI = TI + 4, FJ = TJ + 4;
@@ -67,19 +79,51 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   const T gamma = F32 ? T(g.gamma32) : T(g.gamma);
   const T zpl = F32 ? T(g.zpl32) : T(g.zp_lambda);
 
-  // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj
-  for (int t = threadIdx.x; t < 4 * HI * HJ; t += NT) {
-    const int r = t / (HI * HJ);
-    const int rem = t - r * (HI * HJ);
-    const int hi = rem / HJ, hj = rem - hi * HJ;
-    const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
-    T val = T(0);
-    if (ei < g.nxt && ej < g.nyt) {
-      const double d = a.uin[r * g.plane + (long long)ei * g.pitch + ej];
-      if constexpr (F32) val = f64_to_f32(d);  // integer ALU, not the FP64 pipe
-      else val = d;
+  // FP32 form, stages 2 and 3: start fetching this tile's U^n now; it is
+  // needed only by the RK combination at the end.
+  [[maybe_unused]] const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
+  if constexpr (F32) {
+    if (a.mode == kModeRK && !stage1) {
+      for (int t = threadIdx.x; t < 4 * TI * TJ; t += NT) {
+        const int r = t / (TI * TJ), q = t - r * (TI * TJ);
+        const int i = q / TJ, j = q - (q / TJ) * TJ;
+        if (i0 + i < g.nx && j0 + j < g.ny)
+          cp_async8(&Un64[t], &a.un[r * g.plane + (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j)]);
+      }
     }
-    Us[t] = val;
+  }
+
+  // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj.  All of a
+  // thread's loads are issued before any is used, so they are in flight
+  // together.
+  {
+    constexpr int NLD = (4 * HI * HJ + NT - 1) / NT;
+    double v[NLD];
+#pragma unroll
+    for (int k = 0; k < NLD; ++k) {
+      const int t = threadIdx.x + k * NT;
+      const int r = t / (HI * HJ);
+      const int rem = t - r * (HI * HJ);
+      const int hi = rem / HJ, hj = rem - hi * HJ;
+      const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
+      const bool ok = t < 4 * HI * HJ && ei < g.nxt && ej < g.nyt;
+      v[k] = ok ? __ldg(&a.uin[r * g.plane + (long long)ei * g.pitch + ej]) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < NLD; ++k) {
+      const int t = threadIdx.x + k * NT;
+      if (t < 4 * HI * HJ) {
+        if constexpr (F32) {
+          Us[t] = f64_to_f32(v[k]);  // integer ALU, not the FP64 pipe
+          const int r = t / (HI * HJ);
+          const int rem = t - r * (HI * HJ);
+          const int hi = rem / HJ, hj = rem - hi * HJ;
+          if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) Uin64[(r * TI + hi - 3) * TJ + hj - 3] = v[k];
+        } else {
+          Us[t] = v[k];
+        }
+      }
+    }
   }
   if constexpr (ROUTE) {
     for (int t = threadIdx.x; t < FI * FJ; t += NT) {
@@ -232,7 +276,10 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
   // --- y term, source, RK combination, store
   const double dt = *a.dt;
   [[maybe_unused]] const double cdt = a.c * dt;
-  [[maybe_unused]] const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
+  if constexpr (F32) {
+    cp_async_wait_all();
+    __syncthreads();
+  }
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -256,11 +303,13 @@ __global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
     for (int r = 0; r < 4; ++r) {
       const long long ix = r * g.plane + gidx;
       if constexpr (F32) {
-        // FP64 RK combination; stage 1 (a = 1, b = 0, un == uin) is one FMA
+        // FP64 RK combination from the staged FP64 values; stage 1
+        // (a = 1, b = 0, un == uin) is one FMA
         const double rd = f32_to_f64(rr[r]);
+        const double ui = Uin64[(r * TI + i) * TJ + j];
         if (a.mode == kModeRHS) a.uout[ix] = rd;
-        else if (stage1) a.uout[ix] = fma(cdt, rd, a.un[ix]);
-        else a.uout[ix] = fma(cdt, rd, fma(a.b, a.uin[ix], a.a * a.un[ix]));
+        else if (stage1) a.uout[ix] = fma(cdt, rd, ui);
+        else a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[(r * TI + i) * TJ + j]));
       } else {
         if (a.mode == kModeRHS) {
           a.uout[ix] = double(rr[r]);

@@ -104,10 +104,13 @@ def _constant_net(b3):
 
 
 def test_all_weno_routing_equals_fp32_form():
+    """With every node flagged the routed kernel computes every face with
+    characteristic WENO-Z, i.e. the FP32 form; the two kernel instances may
+    contract multiply-adds differently, so they agree to FP32 rounding."""
     U32, _ = _run(128, 4, 5, wenofd.FP32, 12)
     Uall, frac = _run(128, 4, 5, wenofd.LEARNED, 12, params=_constant_net(50.0))
     assert frac == 1.0
-    assert np.array_equal(U32, Uall)
+    assert np.max(np.abs(Uall - U32)) <= 1e-5 * np.max(np.abs(U32))
 
 
 def test_trained_indicator_gain_over_the_method_without_it():
