@@ -47,9 +47,12 @@ METRIC = "cell-updates/s at 4096^2 (learned+FP32 vs plain FP64 WENO-Z, same GB30
 BYTES_PER_CELL_RK3 = 256
 
 
+TILE_I = 0  # stage-kernel tile height (0: the library default); set by --tile-i
+
+
 def config_for(precision: int, device: int) -> dict:
     return {"TESTCASE": 5, "ELEMNUMX": N, "ELEMNUMY": N, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
-            "SEED": SEED, "PRECISION": precision, "DEVICE": device, "TEND": 1.0e9}
+            "SEED": SEED, "PRECISION": precision, "DEVICE": device, "TEND": 1.0e9, "TILE_I": TILE_I}
 
 
 class ClockSampler:
@@ -233,6 +236,7 @@ def main() -> None:
     ap.add_argument("--fp64-steps", type=int, default=None, help="timed steps of the plain FP64 leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-errors", action="store_true", help="skip the 2x finer reference run")
+    ap.add_argument("--tile-i", type=int, default=0, help="stage-kernel tile height (15 or 31; 0: default)")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (no other legs, errors, e2e or CPU leg): for profiling")
     args = ap.parse_args()
@@ -241,6 +245,8 @@ def main() -> None:
     if args.impl == "reference":
         run_reference_arm(args)
         return
+    global TILE_I
+    TILE_I = args.tile_i
 
     import numpy as np
     import torch

@@ -19,14 +19,15 @@ __device__ __forceinline__ float f64_to_f32(double d) {
   const unsigned hi = unsigned(__double2hiint(d));
   const unsigned lo = unsigned(__double2loint(d));
   const unsigned sign = hi & 0x80000000u;
-  const int e = int((hi >> 20) & 0x7ffu);  // double exponent field
-  const int e32 = e - 896;                  // 1023 - 127
-  const unsigned mant = ((hi & 0x000fffffu) << 3) | (lo >> 29);
-  unsigned bits;
-  if (e32 <= 0) bits = sign;                                             // zero, subnormal, tiny
-  else if (e == 0x7ff) bits = sign | 0x7f800000u | (((hi & 0x000fffffu) | lo) ? 0x400000u : 0u);  // inf / NaN
-  else if (e32 >= 255) bits = sign | 0x7f800000u;                        // beyond FP32 range
-  else bits = sign | (unsigned(e32) << 23) | mant;
+  const unsigned mag = hi & 0x7fffffffu;
+  // rebias the exponent inside the high word (1023 - 127 = 896), then move
+  // exponent and the top 20 mantissa bits up by 3 and append 3 more
+  const unsigned bits = sign | ((mag - 0x38000000u) << 3) | (lo >> 29);
+  if (mag < 0x38100000u) return __uint_as_float(sign);  // zero, subnormal, below 2^-126
+  if (mag >= 0x47f00000u) {                             // beyond FP32 range, inf, NaN
+    const bool nan = mag > 0x7ff00000u || (mag == 0x7ff00000u && lo != 0u);
+    return __uint_as_float(sign | 0x7f800000u | (nan ? 0x400000u : 0u));
+  }
   return __uint_as_float(bits);
 }
 

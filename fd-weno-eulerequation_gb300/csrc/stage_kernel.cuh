@@ -53,8 +53,11 @@ __device__ __forceinline__ T linear_upwind(const T *P, const T *M, int ss) {
   return plus + minus;
 }
 
+// The routed kernel asks for three resident blocks per SM: its per-face
+// characteristic-WENO path runs for a few percent of the faces, so trading
+// registers on that path for occupancy everywhere else pays.
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT) k_stage(Geom g, StageArgs a) {
+__global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
   using S = StageSmem<T, TI, TJ>;
   constexpr int HI = S::HI, HJ = S::HJ;

@@ -1,0 +1,61 @@
+"""Fifth-order convergence of the plain FP64 path on the smooth periodic case,
+and the reference's published convergence rows (README.md:67-74): WENO-JS
+and WENO-Z, SSP-RK3, CFL 0.05, t = 1, L-inf and L1 of density against the
+exact solution 1 + 0.2 sin(pi (x + y - t)), normalised by N^2."""
+import numpy as np
+import pytest
+
+import wenofd
+
+pytestmark = pytest.mark.gpu
+
+# README.md:67-74, printed to three digits
+README = {
+    wenofd.WENOJS: {100: (6.42e-07, 1.92e-07), 120: (2.56e-07, 7.58e-08), 140: (1.17e-07, 3.45e-08),
+                    160: (5.81e-08, 1.74e-08), 180: (3.12e-08, 9.53e-09), 200: (1.78e-08, 5.55e-09)},
+    wenofd.WENOZ: {100: (1.66e-07, 4.21e-08), 120: (6.64e-08, 1.68e-08), 140: (3.06e-08, 7.73e-09),
+                   160: (1.56e-08, 3.95e-09), 180: (8.65e-09, 2.19e-09), 200: (5.10e-09, 1.29e-09)},
+}
+
+
+def _norms(n, scheme, precision=wenofd.FP64, t_end=1.0):
+    with wenofd.Solver({"TESTCASE": 0, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.05,
+                        "SCHEME": scheme, "PRECISION": precision, "TEND": t_end}) as s:
+        s.initialize()
+        s.advance(-1)
+        assert s.info().now == pytest.approx(t_end, abs=1e-9)
+        return s.error_norms()
+
+
+@pytest.mark.parametrize("scheme", [wenofd.WENOZ, wenofd.WENOJS], ids=["wenoz", "wenojs"])
+def test_readme_convergence_table(scheme):
+    errs = {}
+    for n in sorted(README[scheme]):
+        linf, l1, _ = _norms(n, scheme)
+        want_inf, want_l1 = README[scheme][n]
+        # the device FP64 reduction sums in another order than the reference;
+        # three printed digits are far above that difference
+        assert f"{linf:.2e}" == f"{want_inf:.2e}", (n, linf)
+        assert f"{l1:.2e}" == f"{want_l1:.2e}", (n, l1)
+        errs[n] = l1
+    ns = sorted(errs)
+    orders = [np.log(errs[a] / errs[b]) / np.log(b / a) for a, b in zip(ns, ns[1:])]
+    assert min(orders) > 4.7, orders
+
+
+def test_fifth_order_at_t2():
+    """The BASELINE C1 end time t = 2 (the reference hard-codes t = 1)."""
+    l1 = [_norms(n, wenofd.WENOJS, t_end=2.0)[1] for n in (100, 140, 200)]
+    order = np.log(l1[0] / l1[2]) / np.log(2.0)
+    assert order > 4.7, (l1, order)
+
+
+def test_fp32_form_error_floor_is_stated():
+    """FP32 flux arithmetic cannot follow fifth-order convergence down to
+    1e-9: its rounding (about 6e-8 relative in the fluxes, amplified by 1/dx)
+    sets a floor.  The bound below is the stated error of the form on this
+    case."""
+    linf64, l164, _ = _norms(100, wenofd.WENOZ)
+    linf32, l132, _ = _norms(100, wenofd.WENOZ, precision=wenofd.FP32)
+    assert l132 < 5e-6
+    print(f"N=100 WENO-Z L1: FP64 {l164:.3e}, FP32 form {l132:.3e}")
