@@ -227,6 +227,68 @@ def finer_reference_errors(wenofd, params, device: int, n: int = 513, t_end: flo
     return e
 
 
+# Uneven members of the batching leg: seeded four-quadrant Riemann problems.
+BATCH_SHAPES = [(128, 128), (256, 256), (512, 512), (1024, 1024), (192, 320), (384, 256), (96, 640), (768, 512)]
+BATCH_MEMBERS = 64
+
+
+def batching_leg(wenofd, precision: int, device: int, steps: int, warmup: int) -> dict:
+    """Aggregate cell-updates/s of BATCH_MEMBERS independent solves of uneven
+    sizes: one persistent kernel per launch (wenofd_batch_advance, autotuned)
+    against the same solves advanced one at a time (wenofd_advance each,
+    CUDA-graph replays).  Wall clock around the whole advance calls (host
+    checks included in both arms); afterwards the batched members' states are
+    compared with the one-at-a-time states."""
+    import numpy as np
+
+    shapes = [BATCH_SHAPES[k % len(BATCH_SHAPES)] for k in range(BATCH_MEMBERS)]
+
+    def make():
+        out = []
+        for k, (nx, ny) in enumerate(shapes):
+            s = wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
+                               "SEED": 1000 + k, "PRECISION": precision, "DEVICE": device})
+            s.initialize()
+            out.append(s)
+        return out
+
+    cells = sum(nx * ny for nx, ny in shapes)
+    alone = make()
+    for s in alone:
+        s.advance(max_steps=warmup)
+    t0 = time.perf_counter()
+    for s in alone:
+        assert s.advance(max_steps=steps) == steps
+    t_alone = time.perf_counter() - t0
+
+    members = make()
+    b = wenofd.Batch(members)
+    tuned_ms = b.autotune(3)
+    assert b.advance(warmup) == warmup
+    t0 = time.perf_counter()
+    assert b.advance(steps) == steps
+    t_batch = time.perf_counter() - t0
+    info = b.info()
+    diff, l1 = 0.0, 0.0
+    for m, a in zip(members, alone):
+        Um, Ua = m.get_state(), a.get_state()
+        diff = max(diff, float(np.max(np.abs(Um - Ua)) / np.max(np.abs(Ua))))
+        l1 = max(l1, float(np.mean(np.abs(Um - Ua)) / np.mean(np.abs(Ua))))
+    b.close()
+    for s in alone + members:
+        s.close()
+    return {"members": BATCH_MEMBERS, "cells": cells, "steps": steps,
+            "shapes": "seeded Riemann, " + ", ".join(f"{nx}x{ny}" for nx, ny in BATCH_SHAPES) + " (x8 each)",
+            "batched": {"value": steps * cells / t_batch, "unit": "cell-updates/s", "ms_per_step": 1e3 * t_batch / steps},
+            "one_at_a_time": {"value": steps * cells / t_alone, "unit": "cell-updates/s",
+                              "ms_per_step": 1e3 * t_alone / steps},
+            "speedup": t_alone / t_batch,
+            "autotuned": {"tile_i": info.tile_i, "blocks_per_sm": info.blocks_per_sm, "grid": info.grid,
+                          "steps_per_launch": info.steps_per_launch, "graph": info.graph,
+                          "tuned_ms_per_step": tuned_ms},
+            "max_rel_diff_vs_one_at_a_time": diff, "max_l1_rel_diff_vs_one_at_a_time": l1}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -237,6 +299,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-errors", action="store_true", help="skip the 2x finer reference run")
     ap.add_argument("--tile-i", type=int, default=0, help="stage-kernel tile height (15 or 31; 0: default)")
+    ap.add_argument("--no-batching", action="store_true", help="skip the batching leg")
+    ap.add_argument("--only-batching", action="store_true",
+                    help="run the batching leg only (FP32 and FP64 batches vs one at a time): for profiling")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (no other legs, errors, e2e or CPU leg): for profiling")
     args = ap.parse_args()
@@ -275,6 +340,13 @@ def main() -> None:
         t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
+
+    if args.only_batching:
+        out = {"fp32": batching_leg(wenofd, wenofd.FP32, local, args.steps, args.warmup),
+               "fp64": batching_leg(wenofd, wenofd.FP64, local, 2, args.warmup)}
+        if rank == 0:
+            print(json.dumps({"batching": out, "note": "batching leg only (profiling run)"}))
+        return
 
     params, train_info = train_indicator(torch, local)
 
@@ -348,6 +420,12 @@ def main() -> None:
     e2e_value = world * k_e2e * cells / e2e_s
     sl.close()
 
+    # ---- batching: many uneven solves in one persistent launch vs one at a time
+    batching = None
+    if not args.no_batching:
+        batching = {"fp32": batching_leg(wenofd, wenofd.FP32, local, args.steps, args.warmup),
+                    "fp64": batching_leg(wenofd, wenofd.FP64, local, 2, args.warmup)}
+
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline()
@@ -382,6 +460,7 @@ def main() -> None:
                     "h2d_bytes_per_step": 4 * cells * 8, "d2h_bytes_per_step": 4 * cells * 8,
                     "path": "C ABI wenofd_set_state + wenofd_advance(1) + wenofd_get_state, pinned host"},
             "clocks": clocks,
+            "batching": batching,
         }
         if cb is not None:
             line["cpu_baseline"] = cb

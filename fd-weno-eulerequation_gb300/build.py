@@ -38,8 +38,10 @@ CUDA_UNITS = {
     "aux_kernels.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "learned.cu": ["-fmad=false"],
+    "batch_fp64.cu": ["-fmad=false"],
+    "batch_fp32.cu": [],
 }
-CXX_UNITS = ["capi.cpp", "cases.cpp"]
+CXX_UNITS = ["capi.cpp", "cases.cpp", "batch.cpp"]
 
 LIB = os.path.join(OUT, "libwenofd.so")
 EXE = os.path.join(OUT, "wenofd")

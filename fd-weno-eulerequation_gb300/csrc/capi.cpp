@@ -20,38 +20,12 @@
 #include <vector>
 
 #include "cases.h"
+#include "solver.h"
 #include "wenofd_internal.h"
 
 using wenofd::Ctrl;
 using wenofd::Geom;
 using wenofd::StageArgs;
-
-struct wenofd_solver {
-  int device = 0;
-  cudaStream_t stream = nullptr;      // stream in use
-  cudaStream_t own_stream = nullptr;  // created by the handle
-  int testcase = 0, nx = 0, ny = 0, rk = 2, scheme = 1, precision = 0, tile_i = 0;
-  double cfl = 0.5;
-  wenofd::CaseSpec cs;
-  Geom g{};
-  double *S = nullptr, *A = nullptr, *B = nullptr;  // U^n, stage buffers
-  size_t state_bytes = 0;
-  double *special = nullptr;
-  double *partials = nullptr, *red_out = nullptr;
-  Ctrl *ctrl = nullptr;
-  Ctrl *ctrl_host = nullptr;    // pinned mirror
-  double *red_host = nullptr;   // pinned, 4 doubles
-  // learned form (PRECISION 2)
-  unsigned char *flags = nullptr;  // [nxt][pitch], ghosts 1
-  void *ind_weights = nullptr;     // packed BF16 indicator weights
-  int *ind_error = nullptr;
-  float ind_logit_threshold = 0.0f;
-  bool ind_ready = false;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
-  long long graph_kernels = 0;  // kernel nodes in the graph
-  long long launches = 0;       // kernels enqueued so far (graph replays included)
-};
 
 namespace {
 
@@ -669,13 +643,13 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
   s->launches += 1;
   struct St { const double *in, *un; double *out; double a, b, c; };
   std::vector<St> st;
-  if (s->rk == 2)
-    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}, {s->A, s->S, s->B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0},
-          {s->B, s->S, s->S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}};
-  else if (s->rk == 1)
-    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}, {s->A, s->S, s->S, 0.5, 0.5, 0.5}};
-  else
-    st = {{s->S, s->S, s->A, 1.0, 0.0, 1.0}};
+  st.push_back({s->S, s->S, s->A, 1.0, 0.0, 1.0});
+  if (s->rk == 2) {
+    st.push_back({s->A, s->S, s->B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0});
+    st.push_back({s->B, s->S, s->S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0});
+  } else if (s->rk == 1) {
+    st.push_back({s->A, s->S, s->S, 0.5, 0.5, 0.5});
+  }
   cudaEvent_t e0, e1;
   CUDA_TRY(cudaEventCreate(&e0));
   CUDA_TRY(cudaEventCreate(&e1));

@@ -53,15 +53,18 @@ __device__ __forceinline__ T linear_upwind(const T *P, const T *M, int ss) {
   return plus + minus;
 }
 
-// The routed kernel asks for three resident blocks per SM: its per-face
-// characteristic-WENO path runs for a few percent of the faces, so trading
-// registers on that path for occupancy everywhere else pays.
-template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a) {
-  if (*a.active == 0) return;
+// One tile (TI x TJ interior nodes starting at i0, j0) of one RK stage,
+// executed by all NT threads of a block; smem_raw holds StageSmem::bytes.
+// Shared by the per-solve kernel k_stage and the persistent batched kernel.
+// COH: the tile's inputs may have been written earlier in the same kernel by
+// other blocks (the persistent batched kernel): loads then go through L2
+// only (ld.global.cg) instead of the non-coherent read-only path, and U^n is
+// loaded in the epilogue instead of being prefetched with cp.async.
+template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false>
+__device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, const int i0, const int j0,
+                                           unsigned char *smem_raw) {
   using S = StageSmem<T, TI, TJ>;
   constexpr int HI = S::HI, HJ = S::HJ;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T *Us = reinterpret_cast<T *>(smem_raw);
   T *Fp = Us + S::kU;
   T *Fm = Fp + S::kSplit;
@@ -76,8 +79,6 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
   __shared__ short slist[ROUTE ? kMaxFaces : 1];
   __shared__ int scount;
 
-  const int i0 = blockIdx.y * TI;  // first interior node of the tile (0-based)
-  const int j0 = blockIdx.x * TJ;
   constexpr bool F32 = sizeof(T) == 4;
   const T gamma = F32 ? T(g.gamma32) : T(g.gamma);
   const T zpl = F32 ? T(g.zpl32) : T(g.zp_lambda);
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
   // FP32 form, stages 2 and 3: start fetching this tile's U^n now; it is
   // needed only by the RK combination at the end.
   [[maybe_unused]] const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
-  if constexpr (F32) {
+  if constexpr (F32 && !COH) {
     if (a.mode == kModeRK && !stage1) {
       for (int t = threadIdx.x; t < 4 * TI * TJ; t += NT) {
         const int r = t / (TI * TJ), q = t - r * (TI * TJ);
@@ -110,7 +111,9 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
       const int hi = rem / HJ, hj = rem - hi * HJ;
       const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
       const bool ok = t < 4 * HI * HJ && ei < g.nxt && ej < g.nyt;
-      v[k] = ok ? __ldg(&a.uin[r * g.plane + (long long)ei * g.pitch + ej]) : 0.0;
+      const double *src = &a.uin[r * g.plane + (long long)ei * g.pitch + ej];
+      if constexpr (COH) v[k] = ok ? __ldcg(src) : 0.0;
+      else v[k] = ok ? __ldg(src) : 0.0;
     }
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
@@ -277,9 +280,9 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
   __syncthreads();
 
   // --- y term, source, RK combination, store
-  const double dt = *a.dt;
+  const double dt = COH ? __ldcg(a.dt) : *a.dt;
   [[maybe_unused]] const double cdt = a.c * dt;
-  if constexpr (F32) {
+  if constexpr (F32 && !COH) {
     cp_async_wait_all();
     __syncthreads();
   }
@@ -312,17 +315,29 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
         const double ui = Uin64[(r * TI + i) * TJ + j];
         if (a.mode == kModeRHS) a.uout[ix] = rd;
         else if (stage1) a.uout[ix] = fma(cdt, rd, ui);
+        else if constexpr (COH) a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
         else a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[(r * TI + i) * TJ + j]));
       } else {
         if (a.mode == kModeRHS) {
           a.uout[ix] = double(rr[r]);
         } else {
-          const double un = a.un[ix], ui = a.uin[ix];
+          const double un = COH ? __ldcg(&a.un[ix]) : a.un[ix], ui = COH ? __ldcg(&a.uin[ix]) : a.uin[ix];
           a.uout[ix] = a.a * un + a.b * ui + a.c * dt * double(rr[r]);
         }
       }
     }
   }
+}
+
+// The routed kernel asks for three resident blocks per SM: its per-face
+// characteristic-WENO path runs for a few percent of the faces, so trading
+// registers on that path for occupancy everywhere else pays.
+template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
+__global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a) {
+  if (*a.active == 0) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // first interior node of the tile (0-based)
+  stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
 }
 
 // Host-side launcher for one precision: picks the kernel instance for the

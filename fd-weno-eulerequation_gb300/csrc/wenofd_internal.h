@@ -71,6 +71,55 @@ Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lam
 cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
 cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
 
+// batch_fp64.cu / batch_fp32.cu: the persistent batched kernel
+// (batch_kernel.cuh).  tile_i 0 = default; grid receives the launch's block
+// count; with b.members null nothing is launched (grid query only).
+// One member of a batch (device-resident array of these).
+struct BatchMember {
+  Geom g;
+  double *S, *A, *B;
+  const double *special;
+  Ctrl *ctrl;
+  int tiles_j;  // tiles along y; tiles along x = ceil(nx / TI)
+};
+
+// Exclusive prefix sums of work items per member (n+1 entries each).
+struct BatchWork {
+  const int *tile_prefix;  // stage tiles (depends on TI)
+  const int *bc_prefix;    // ghost-fill chunks of kBcChunk entries
+  const int *pt_prefix;    // time-step chunks of kPtChunk nodes
+};
+
+constexpr int kBcChunk = 256;
+constexpr int kPtChunk = 4096;
+constexpr int kBatchPhases = 8;  // work counters per step: dt x 2, (bc, stage) x 3
+constexpr unsigned kBarrierLimit = 1u << 24;
+
+struct BatchArgs {
+  BatchMember *members;
+  BatchWork work;
+  int n;               // members
+  int nsteps;          // steps per launch
+  unsigned *counters;  // nsteps * kBatchPhases work counters, zeroed before the launch
+  unsigned *barrier;   // [0] arrivals (zero before the launch), [1] generation
+  int *error;          // set if a barrier wait gave up
+  int *status;         // after the launch: [0] members that can still step, [1] any member error
+};
+
+// Per-member summary gathered for the host in one copy.
+struct BatchMemberStatus {
+  double now;
+  long long steps;
+  int error, done;
+};
+
+cudaError_t launch_batch_fp64(const BatchArgs &b, int scheme, int tile_i, int blocks_per_sm, cudaStream_t s,
+                              int *grid);
+cudaError_t launch_batch_fp32(const BatchArgs &b, int scheme, int tile_i, int blocks_per_sm, cudaStream_t s,
+                              int *grid);
+cudaError_t launch_batch_setup(BatchMember *members, int n, long long max_steps, cudaStream_t s);
+cudaError_t launch_batch_gather(const BatchMember *members, int n, BatchMemberStatus *out, cudaStream_t s);
+
 // learned.cu: indicator features, labels, tensor-core inference
 size_t indicator_weights_bytes();
 void pack_indicator_weights(const float *params, void *host_out);

@@ -49,6 +49,14 @@ class Info(C.Structure):
     ]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("members", C.c_int), ("precision", C.c_int), ("tile_i", C.c_int), ("blocks_per_sm", C.c_int),
+        ("grid", C.c_int), ("steps_per_launch", C.c_int), ("graph", C.c_int),
+        ("cells", C.c_longlong), ("launches", C.c_longlong), ("tuned_ms_per_step", C.c_double),
+    ]
+
+
 _lib = None
 
 
@@ -92,6 +100,15 @@ def lib() -> C.CDLL:
         D = C.c_double
         L.wenofd_calc_dt_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, D, D, D, D, D, D, C.c_void_p,
                                              C.c_void_p]
+        L.wenofd_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
+        L.wenofd_batch_destroy.argtypes = [H]
+        L.wenofd_batch_configure.argtypes = [H, C.c_int, C.c_int, C.c_int]
+        L.wenofd_batch_autotune.argtypes = [H, C.c_int, P]
+        L.wenofd_batch_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
+        L.wenofd_batch_get_info.argtypes = [H, C.POINTER(BatchInfo)]
+        for f in ("wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
+                  "wenofd_batch_advance", "wenofd_batch_get_info"):
+            getattr(L, f).restype = C.c_int
         for f in ("wenofd_create", "wenofd_create_from_file", "wenofd_destroy", "wenofd_set_stream",
                   "wenofd_get_info", "wenofd_initialize", "wenofd_fill_boundary", "wenofd_set_state",
                   "wenofd_get_state", "wenofd_get_state_ghosted", "wenofd_get_flux", "wenofd_calc_dt",
@@ -254,6 +271,52 @@ class Solver:
         return out
 
 
+class Batch:
+    """Many Solver handles advanced together by one persistent kernel
+    (wenofd_batch_*).  Members keep their own state: read it through them."""
+
+    def __init__(self, members: list[Solver]):
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m._h for m in self.members])
+        self._h = C.c_void_p()
+        _check(lib().wenofd_batch_create(arr, len(self.members), C.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            lib().wenofd_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def configure(self, tile_i: int = 0, blocks_per_sm: int = 0, steps_per_launch: int = 0) -> None:
+        _check(lib().wenofd_batch_configure(self._h, tile_i, blocks_per_sm, steps_per_launch))
+
+    def autotune(self, steps: int = 3) -> float:
+        ms = C.c_double()
+        _check(lib().wenofd_batch_autotune(self._h, steps, C.byref(ms)))
+        return ms.value
+
+    def advance(self, max_steps: int = -1) -> int:
+        n = C.c_longlong()
+        _check(lib().wenofd_batch_advance(self._h, max_steps, C.byref(n)))
+        return n.value
+
+    def info(self) -> BatchInfo:
+        i = BatchInfo()
+        _check(lib().wenofd_batch_get_info(self._h, C.byref(i)))
+        return i
+
+
 EXPORTED = [
     "wenofd_last_error", "wenofd_version", "wenofd_create", "wenofd_create_from_file", "wenofd_destroy",
     "wenofd_set_stream", "wenofd_get_info", "wenofd_initialize", "wenofd_set_state", "wenofd_get_state",
@@ -262,6 +325,8 @@ EXPORTED = [
     "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
     "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values", "wenofd_set_indicator", "wenofd_indicator_flags",
     "wenofd_indicator_data", "wenofd_mlp_forward", "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train",
+    "wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
+    "wenofd_batch_advance", "wenofd_batch_get_info",
 ]
 
 

@@ -181,6 +181,55 @@ int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *dev_m, floa
 int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs, int batch,
                      float lr, unsigned long long seed, float *host_epoch_loss, void *stream);
 
+/* ---- Batches: many independent solves in one persistent launch ----------
+ * No counterpart in the reference, which runs one solve per program
+ * (src/main.cpp:8-30); a batch replaces N runs of the time loop of
+ * CWENOFD::run (src/WENOFD.cpp:213-224, calculateDeltaT + RunRK3 + m_now += dt)
+ * by one kernel launch per few steps that advances every member.
+ *
+ * Members are existing handles: same device, same SCHEME, RKMETH 2
+ * (SSP-RK3) and PRECISION FP64 or FP32 (the learned form is not batched);
+ * sizes, test cases, boundary conditions, CFL and TEND may differ.  The
+ * batch works on the members' own device state: a member stepped by a
+ * batch is read (wenofd_get_state, wenofd_get_info, ...) through its own
+ * handle; members must outlive the batch and must not be advanced through
+ * their own handles while a batch call runs.  Each member's steps are
+ * those of wenofd_advance on its own: FP64 members bit for bit.
+ *
+ * wenofd_batch_configure: tile rows per stage tile (FP64: 7 or 15, FP32: 15
+ *   or 31; 0 = default 15), resident blocks per SM (0 = as many as fit) and
+ *   steps per launch (0 = chosen from the batch's size).
+ * wenofd_batch_autotune: times each (tile, blocks per SM) candidate over
+ *   `steps` steps, keeps the fastest and returns its milliseconds per step;
+ *   the members' states and times are restored after every trial.
+ * wenofd_batch_advance: like wenofd_advance for every member: each member
+ *   steps until its TEND or `max_steps` more steps (-1: no limit).
+ *   *steps_done receives the largest number of steps a member took.
+ *   WENOFD_NAN_DT if a member's time step became NaN (that member stops,
+ *   the others finish the call; the message names the member index);
+ *   WENOFD_TIMEOUT if a grid barrier wait gave up. */
+typedef struct wenofd_batch wenofd_batch;
+
+typedef struct wenofd_batch_info {
+  int members;
+  int precision;
+  int tile_i;            /* tile rows of the stage tiles */
+  int blocks_per_sm;     /* resident blocks per SM of the persistent kernel */
+  int grid;              /* blocks per launch */
+  int steps_per_launch;  /* time steps one launch runs */
+  int graph;             /* 1: launches are replays of a captured CUDA graph */
+  long long cells;       /* interior nodes over all members */
+  long long launches;    /* kernels launched by this batch so far */
+  double tuned_ms_per_step; /* from wenofd_batch_autotune, else 0 */
+} wenofd_batch_info;
+
+int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out);
+int wenofd_batch_destroy(wenofd_batch *b);
+int wenofd_batch_configure(wenofd_batch *b, int tile_i, int blocks_per_sm, int steps_per_launch);
+int wenofd_batch_autotune(wenofd_batch *b, int steps, double *ms_per_step);
+int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_done);
+int wenofd_batch_get_info(const wenofd_batch *b, wenofd_batch_info *info);
+
 /* No counterpart in the reference.  calculateDeltaT (src/WENOFD.cpp:398-452
  * arithmetic, bit for bit) of a caller-owned device state, for callers that
  * must not allocate: an application whose GPU memory belongs to its own pool

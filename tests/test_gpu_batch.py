@@ -1,0 +1,202 @@
+"""Batches: independent solves of different sizes, cases and boundary
+conditions advanced by one persistent kernel (wenofd_batch_*).
+
+A member's steps are those of wenofd_advance on its own handle: FP64 members
+bit for bit (and so the oracle's).  FP32 members run the same FP32 stage
+code compiled into another kernel, where the compiler may contract a
+different set of FP32 multiply-adds, so they are held to the FP32 form's own
+accepted error against the FP64 solve (the bound of the FP32 form's tests)."""
+import numpy as np
+import pytest
+
+import oracle as orc
+import wenofd
+
+pytestmark = pytest.mark.gpu
+
+FP32_REL_TOL = 1e-5  # max |U32 - U64| / max |U64| after the steps below
+
+# (testcase, nx, ny, seed, extra keys): uneven sizes, periodic / slip /
+# SPECIAL / symmetric boundaries, gravity (RTI)
+MEMBERS = [
+    (orc.RIEMANN_SEEDED, 48, 40, 3, {}),
+    (orc.SMOOTH, 64, 64, 0, {}),
+    (orc.SHEAR, 100, 37, 5, {}),
+    (orc.RIEMANN1, 33, 90, 0, {}),
+    (orc.RTI, 24, 96, 0, {}),
+    (orc.RIEMANN2, 130, 70, 0, {}),
+]
+
+
+def _cfg(tc, nx, ny, seed, extra, precision, scheme=orc.WENOZ, tend=None):
+    c = {"TESTCASE": tc, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.6, "SCHEME": scheme,
+         "SEED": seed, "PRECISION": precision}
+    c.update(extra)
+    if tend is not None:
+        c["TEND"] = tend
+    return c
+
+
+def _alone(cfgs, max_steps):
+    out = []
+    for c in cfgs:
+        with wenofd.Solver(c) as s:
+            s.initialize()
+            n = s.advance(max_steps=max_steps)
+            out.append((s.get_state(), s.info().now, n))
+    return out
+
+
+def _batched(cfgs, max_steps, configure=None, autotune=0):
+    solvers = [wenofd.Solver(c) for c in cfgs]
+    try:
+        for s in solvers:
+            s.initialize()
+        with wenofd.Batch(solvers) as b:
+            if configure:
+                b.configure(**configure)
+            if autotune:
+                b.autotune(autotune)
+            n = b.advance(max_steps)
+            info = b.info()
+        return [(s.get_state(), s.info().now, s.info().steps) for s in solvers], n, info
+    finally:
+        for s in solvers:
+            s.close()
+
+
+@pytest.mark.parametrize("configure", [None, {"tile_i": 7}, {"steps_per_launch": 5}, {"blocks_per_sm": 1}],
+                         ids=["default", "tile7", "launch5", "bps1"])
+def test_fp64_batch_bitwise_equals_single_solves(configure):
+    cfgs = [_cfg(*m, wenofd.FP64) for m in MEMBERS]
+    steps = 12
+    ref = _alone(cfgs, steps)
+    got, n, info = _batched(cfgs, steps, configure)
+    assert n == steps
+    assert info.members == len(cfgs) and info.cells == sum(m[1] * m[2] for m in MEMBERS)
+    for (U, now, k), (Ur, nowr, kr) in zip(got, ref):
+        assert k == kr == steps
+        assert now == nowr
+        assert np.array_equal(U, Ur)
+
+
+def test_fp64_batch_member_matches_oracle():
+    tc, nx, ny, seed, extra = MEMBERS[0]
+    p = orc.Problem(tc, nx, ny, orc.WENOZ, 2, 0.6, seed=seed)
+    p.run(max_steps=8)
+    got, n, _ = _batched([_cfg(*MEMBERS[0], wenofd.FP64), _cfg(*MEMBERS[2], wenofd.FP64)], 8)
+    assert n == 8
+    assert np.array_equal(got[0][0], p.interior())
+    assert got[0][1] == p.now
+
+
+@pytest.mark.parametrize("scheme", [orc.WENOJS, orc.WENOZP, orc.WENOZPI])
+def test_fp64_batch_other_schemes(scheme):
+    cfgs = [_cfg(*m, wenofd.FP64, scheme=scheme) for m in MEMBERS[:4]]
+    ref = _alone(cfgs, 6)
+    got, n, _ = _batched(cfgs, 6)
+    assert n == 6
+    for (U, now, _), (Ur, nowr, _) in zip(got, ref):
+        assert now == nowr and np.array_equal(U, Ur)
+
+
+@pytest.mark.parametrize("configure", [None, {"tile_i": 31}], ids=["default", "tile31"])
+def test_fp32_batch_close_to_single_solves(configure):
+    steps = 12
+    ref64 = _alone([_cfg(*m, wenofd.FP64) for m in MEMBERS], steps)
+    cfgs = [_cfg(*m, wenofd.FP32) for m in MEMBERS]
+    alone32 = _alone(cfgs, steps)
+    got, n, _ = _batched(cfgs, steps, configure)
+    assert n == steps
+    for (U, now, k), (U1, now1, k1), (Ur, nowr, _) in zip(got, alone32, ref64):
+        assert k == k1 == steps
+        assert np.all(np.isfinite(U))
+        scale = np.max(np.abs(Ur))
+        assert np.max(np.abs(U - Ur)) / scale <= FP32_REL_TOL
+        assert np.max(np.abs(U1 - Ur)) / scale <= FP32_REL_TOL
+        assert abs(now - nowr) <= FP32_REL_TOL * nowr
+
+
+def test_members_stop_at_their_own_end_time():
+    """advance(-1): every member runs to its own TEND, as wenofd_advance does."""
+    tends = [0.004, 0.011, 0.002]
+    cfgs = [_cfg(*m, wenofd.FP64, tend=t) for m, t in zip(MEMBERS[:3], tends)]
+    ref = _alone(cfgs, -1)
+    got, n, _ = _batched(cfgs, -1)
+    assert n == max(r[2] for r in ref)
+    for (U, now, k), (Ur, nowr, kr), t in zip(got, ref, tends):
+        assert k == kr and now == nowr and abs(now - t) <= 1e-9
+        assert np.array_equal(U, Ur)
+
+
+@pytest.mark.parametrize("precision", [wenofd.FP64, wenofd.FP32])
+def test_autotune_restores_state_and_keeps_results(precision):
+    cfgs = [_cfg(*m, precision) for m in MEMBERS]
+    ref, _, _ = _batched(cfgs, 5)
+    solvers = [wenofd.Solver(c) for c in cfgs]
+    try:
+        for s in solvers:
+            s.initialize()
+        before = [s.get_state() for s in solvers]
+        with wenofd.Batch(solvers) as b:
+            ms = b.autotune(3)
+            info = b.info()
+            assert ms > 0 and info.tuned_ms_per_step == ms
+            assert info.tile_i in ((7, 15) if precision == wenofd.FP64 else (15, 31))
+            for s, U0 in zip(solvers, before):
+                assert s.info().steps == 0 and s.info().now == 0.0
+                assert np.array_equal(s.get_state(), U0)
+            assert b.advance(5) == 5
+        for s, (Ur, nowr, _) in zip(solvers, ref):
+            U = s.get_state()
+            if precision == wenofd.FP64:
+                assert s.info().now == nowr and np.array_equal(U, Ur)
+            else:  # the tuned tile height may select the other FP32 kernel instance
+                assert np.max(np.abs(U - Ur)) / np.max(np.abs(Ur)) <= FP32_REL_TOL
+    finally:
+        for s in solvers:
+            s.close()
+
+
+def test_nan_member_stops_and_others_finish():
+    cfgs = [_cfg(*m, wenofd.FP64) for m in MEMBERS[:3]]
+    ref = _alone(cfgs, 4)
+    solvers = [wenofd.Solver(c) for c in cfgs]
+    try:
+        for s in solvers:
+            s.initialize()
+        U = solvers[1].get_state()
+        U[0, 5, 7] = np.nan
+        solvers[1].set_state(U)
+        with wenofd.Batch(solvers) as b:
+            with pytest.raises(wenofd.WenofdError) as ei:
+                b.advance(4)
+        assert ei.value.status == wenofd.NAN_DT and "member 1" in str(ei.value)
+        assert solvers[1].info().steps == 0
+        for k in (0, 2):
+            assert solvers[k].info().steps == 4
+            assert np.array_equal(solvers[k].get_state(), ref[k][0])
+    finally:
+        for s in solvers:
+            s.close()
+
+
+def test_batch_rejects_mixed_or_unsupported_members():
+    a = wenofd.Solver(_cfg(*MEMBERS[0], wenofd.FP64))
+    b = wenofd.Solver(_cfg(*MEMBERS[1], wenofd.FP64, scheme=orc.WENOJS))
+    c = wenofd.Solver(_cfg(*MEMBERS[1], wenofd.FP32))
+    d = wenofd.Solver(_cfg(*MEMBERS[1], wenofd.LEARNED))
+    e = wenofd.Solver(dict(_cfg(*MEMBERS[1], wenofd.FP64), RKMETH=1))
+    try:
+        for bad in ([a, b], [a, c], [d], [a, e], [a, a]):
+            with pytest.raises(wenofd.WenofdError) as ei:
+                wenofd.Batch(bad)
+            assert ei.value.status == wenofd.BAD_ARG
+        with wenofd.Batch([a]) as bt:
+            for kw in ({"tile_i": 31}, {"tile_i": 9}, {"blocks_per_sm": -1}):
+                with pytest.raises(wenofd.WenofdError) as ei:
+                    bt.configure(**kw)
+                assert ei.value.status == wenofd.BAD_ARG
+    finally:
+        for s in (a, b, c, d, e):
+            s.close()
