@@ -87,6 +87,8 @@ def lib() -> C.CDLL:
         L.orc_special_table.argtypes = [C.POINTER(Case), C.POINTER(Grid), P]
         L.orc_fill_boundary.argtypes = [C.POINTER(Grid), P]
         L.orc_assemble_rhs.argtypes = [C.POINTER(Grid), P, P]
+        L.orc_fill_boundary_slab.argtypes = [C.POINTER(Grid), P, I, I]
+        L.orc_assemble_rhs_ghosted.argtypes = [C.POINTER(Grid), P, P]
         L.orc_calc_dt.restype = I
         L.orc_calc_dt.argtypes = [C.POINTER(Grid), P, D, D, D, P]
         L.orc_rk_step.argtypes = [C.POINTER(Grid), I, P, P, P, D]
@@ -215,3 +217,42 @@ class Problem:
 
 def ref_available() -> bool:
     return os.path.exists(REF_BIN)
+
+
+class Slab:
+    """One rank's x-slab of a Problem, as the reference's MPI ranks hold it
+    (src/WENOFD.cpp:36-70): nodes [start, start + count) of the x interior
+    with 4 ghost columns each side, all y nodes.  Used by the multi-rank
+    tests as the per-rank compute; the ghost exchange between ranks is the
+    product's (wenofd.partition)."""
+
+    def __init__(self, prob: "Problem", start: int, count: int):
+        self.prob, self.start, self.count = prob, start, count
+        self.grid = Grid()
+        C.memmove(C.byref(self.grid), C.byref(prob.grid), C.sizeof(Grid))
+        self.grid.nx = count
+        nxt_g, nyt = prob.nx + 2 * NG, prob.ny + 2 * NG
+        cols = slice(start, start + count + 2 * NG)
+        ytab = prob.special[:8 * nxt_g].reshape(8, nxt_g)[:, cols]
+        self.special = np.concatenate([ytab.reshape(-1), prob.special[8 * nxt_g:8 * nxt_g + 8 * nyt]])
+        self.grid.special = _p(self.special)
+        self.U = np.ascontiguousarray(prob.U[:, cols, :])
+        self.Un = np.zeros_like(self.U)
+        self.rhs = np.zeros_like(self.U)
+
+    def interior(self, A: np.ndarray | None = None) -> np.ndarray:
+        A = self.U if A is None else A
+        return A[:, NG:NG + self.count, NG:NG + self.prob.ny].copy()
+
+    def fill_boundary(self, left_edge: bool, right_edge: bool) -> None:
+        lib().orc_fill_boundary_slab(C.byref(self.grid), _p(self.U), int(left_edge), int(right_edge))
+
+    def assemble_rhs(self) -> np.ndarray:
+        lib().orc_assemble_rhs_ghosted(C.byref(self.grid), _p(self.U), _p(self.rhs))
+        return self.interior(self.rhs)
+
+    def local_dt(self, cfl: float, now: float, t_end: float) -> float:
+        dt = np.zeros(1)
+        lib().orc_calc_dt(C.byref(self.grid), _p(self.U), cfl, now, t_end, _p(dt))
+        return float(dt[0])
+

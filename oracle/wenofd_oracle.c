@@ -486,7 +486,6 @@ void orc_special_table(const orc_case *c, const orc_grid *g, double *tab) {
  * setBoundary then fills y over every column with the BOTTOM condition for
  * both sides (line 1009), then x over every row for non-periodic sides. */
 void orc_fill_boundary(const orc_grid *g, double *U) {
-  const int nxt = NXT(g), nyt = NYT(g);
   const int sx = ORC_NG, ex = ORC_NG + g->nx, sy = ORC_NG, ey = ORC_NG + g->ny;
   for (int k = 1; k <= ORC_NG; ++k)
     for (int ej = sy; ej < ey; ++ej)
@@ -494,6 +493,18 @@ void orc_fill_boundary(const orc_grid *g, double *U) {
         AT(g, U, r, sx - k, ej) = AT(g, U, r, ex - 1 - k, ej);
         AT(g, U, r, ex - 1 + k, ej) = AT(g, U, r, sx + k, ej);
       }
+  orc_fill_boundary_slab(g, U, 1, 1);
+}
+
+/* setBoundary of one rank's x-slab (src/WENOFD.cpp:998-1159) after its x
+ * ghost columns of the interior rows were exchanged: the y conditions over
+ * every column, ghost columns included, then the x conditions on the sides
+ * that are domain edges (left_edge: rank 0, right_edge: the last rank) over
+ * every row.  On a slab grid g->nx is the slab's node count and the SPECIAL
+ * table is the slab's slice (y part [8][slab nx + 8], x part as global). */
+void orc_fill_boundary_slab(const orc_grid *g, double *U, int left_edge, int right_edge) {
+  const int nxt = NXT(g), nyt = NYT(g);
+  const int sx = ORC_NG, ex = ORC_NG + g->nx, sy = ORC_NG, ey = ORC_NG + g->ny;
   for (int ei = 0; ei != nxt; ei++) {
     for (int e1 = 1; e1 <= ORC_NG; ++e1) {
       switch (g->bc_bottom) {
@@ -523,7 +534,7 @@ void orc_fill_boundary(const orc_grid *g, double *U) {
       }
     }
   }
-  for (int ej = 0; ej != nyt; ej++) {
+  for (int ej = 0; ej != nyt && left_edge; ej++) {
     for (int e1 = 1; e1 <= ORC_NG; ++e1) {
       switch (g->bc_left) {
         case ORC_SYMMETRIC:
@@ -539,7 +550,7 @@ void orc_fill_boundary(const orc_grid *g, double *U) {
       }
     }
   }
-  for (int ej = 0; ej != nyt; ej++) {
+  for (int ej = 0; ej != nyt && right_edge; ej++) {
     for (int e1 = 1; e1 <= ORC_NG; ++e1) {
       switch (g->bc_right) {
         case ORC_SYMMETRIC:
@@ -601,12 +612,18 @@ static void face_flux(const orc_grid *g, int dir, const double Um[4], const doub
  * (481-798) + assembleSourceTerm (800-821).  Fills U's ghosts; rhs is a full
  * array whose interior is written. */
 void orc_assemble_rhs(const orc_grid *g, double *U, double *rhs) {
+  orc_fill_boundary(g, U);
+  orc_assemble_rhs_ghosted(g, U, rhs);
+}
+
+/* The same with U's ghosts already filled (an x-slab after its exchange and
+ * orc_fill_boundary_slab). */
+void orc_assemble_rhs_ghosted(const orc_grid *g, const double *U, double *rhs) {
   const int nxt = NXT(g), nyt = NYT(g);
   const int sx = ORC_NG, ex = ORC_NG + g->nx, sy = ORC_NG, ey = ORC_NG + g->ny;
   for (int r = 0; r < 4; ++r)
     for (int ei = sx; ei < ex; ++ei)
       for (int ej = sy; ej < ey; ++ej) AT(g, rhs, r, ei, ej) = 0.0;
-  orc_fill_boundary(g, U);
 
   const int nmax = nxt > nyt ? nxt : nyt;
   /* Lines are independent, so they are spread over threads; each face is

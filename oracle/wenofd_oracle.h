@@ -80,7 +80,9 @@ void orc_special_table(const orc_case *c, const orc_grid *g, double *tab);
 
 /* the hot path */
 void orc_fill_boundary(const orc_grid *g, double *U);
+void orc_fill_boundary_slab(const orc_grid *g, double *U, int left_edge, int right_edge);
 void orc_assemble_rhs(const orc_grid *g, double *U, double *rhs);
+void orc_assemble_rhs_ghosted(const orc_grid *g, const double *U, double *rhs);
 int orc_calc_dt(const orc_grid *g, const double *U, double cfl, double now, double t_end, double *dt);
 void orc_rk_step(const orc_grid *g, int rk, double *U, double *Un, double *rhs, double dt);
 int orc_run(const orc_grid *g, int rk, double cfl, double *U, double *Un, double *rhs, double *now,
