@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 512 / NT : 1) k_batch(Bat
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
         a.flags = nullptr;
-        stage_tile<T, SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
+        if constexpr (F32) stage_tile_f32<SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
+        else stage_tile<T, SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < 2) {
         grid_barrier(b, Nothing());
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 512 / NT : 1) k_batch(Bat
 // from that query.
 template <typename T, int TI, int NT>
 cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm, cudaStream_t s, int *grid) {
-  using Sm = StageSmem<T, TI, 32>;
+  constexpr size_t smem = stage_smem_bytes<T, TI, 32>();
   void (*fn)(BatchArgs) = nullptr;
   switch (scheme) {
     case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT>; break;
@@ -327,12 +328,12 @@ cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm,
   if (!grid) return cudaErrorInvalidValue;
   cudaError_t e;
   if (!b.members) {
-    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Sm::bytes))) != cudaSuccess)
+    if ((e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem))) != cudaSuccess)
       return e;
     int dev = 0, sms = 0, occ = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, NT, Sm::bytes)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, NT, smem)) != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     *grid = sms * (blocks_per_sm > 0 && blocks_per_sm < occ ? blocks_per_sm : occ);
     return cudaSuccess;
@@ -341,7 +342,7 @@ cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm,
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(*grid);
   cfg.blockDim = dim3(NT);
-  cfg.dynamicSmemBytes = Sm::bytes;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -218,11 +218,39 @@ __device__ __forceinline__ T weno(T a, T b, T c, T d, T e, T zp_lambda) {
 // from one set of (u, v, p, c, B1, B2, H): the reference recomputes them per
 // matrix from the same inputs, which gives identical values.
 //
+// fp(s, r) / fm(s, r): component r of F+ at node face-3+s and of F- at node
+// face-2+s, s = 0..4.
+template <typename T>
+struct StridedStencil {  // SoA: nodes `ss` elements apart, components `cs` apart
+  const T *p;
+  int ss, cs;
+  __device__ __forceinline__ T operator()(int s, int r) const { return p[s * ss + r * cs]; }
+};
+struct Float4Stencil {  // AoS: one float4 per node, nodes `ss` float4s apart
+  const float4 *p;
+  int ss;
+  __device__ __forceinline__ float operator()(int s, int r) const {
+    const float4 v = p[s * ss];
+    return r == 0 ? v.x : (r == 1 ? v.y : (r == 2 ? v.z : v.w));
+  }
+};
+
+template <typename T, int DIR, int SCHEME, typename St>
+__device__ __forceinline__ void face_flux_st(T gamma, T zp_lambda, const T um[4], const T u0[4], const St &fp,
+                                             const St &fm, T out[4]);
+
 // fp / fm point at F+ of node face-3 and F- of node face-2, component 0;
 // consecutive stencil nodes are `ss` elements apart, components `cs` apart.
 template <typename T, int DIR, int SCHEME>
 __device__ __forceinline__ void face_flux(T gamma, T zp_lambda, const T um[4], const T u0[4],
                                           const T *fp, const T *fm, int ss, int cs, T out[4]) {
+  face_flux_st<T, DIR, SCHEME>(gamma, zp_lambda, um, u0, StridedStencil<T>{fp, ss, cs},
+                               StridedStencil<T>{fm, ss, cs}, out);
+}
+
+template <typename T, int DIR, int SCHEME, typename St>
+__device__ __forceinline__ void face_flux_st(T gamma, T zp_lambda, const T um[4], const T u0[4], const St &fp,
+                                             const St &fm, T out[4]) {
   T ave[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) ave[r] = T(0.5) * (um[r] + u0[r]);
@@ -255,17 +283,15 @@ __device__ __forceinline__ void face_flux(T gamma, T zp_lambda, const T um[4], c
     T vp[5], vm[5];
 #pragma unroll
     for (int s = 0; s < 5; ++s) {
-      const T *P = fp + s * ss;
-      const T *M = fm + s * ss;
-      T x = l0 * P[0];
-      x += l1 * P[cs];
-      x += l2 * P[2 * cs];
-      x += l3 * P[3 * cs];
+      T x = l0 * fp(s, 0);
+      x += l1 * fp(s, 1);
+      x += l2 * fp(s, 2);
+      x += l3 * fp(s, 3);
       vp[s] = x;
-      T y = l0 * M[0];
-      y += l1 * M[cs];
-      y += l2 * M[2 * cs];
-      y += l3 * M[3 * cs];
+      T y = l0 * fm(s, 0);
+      y += l1 * fm(s, 1);
+      y += l2 * fm(s, 2);
+      y += l3 * fm(s, 3);
       vm[s] = y;
     }
     const T hp = weno<T, SCHEME>(vp[0], vp[1], vp[2], vp[3], vp[4], zp_lambda);

@@ -1,0 +1,280 @@
+// One RK stage tile of the FP32 precision form (and of the learned form,
+// ROUTE), the FP32 counterpart of stage_tile in stage_kernel.cuh with the
+// same phases and the same per-face arithmetic, laid out for the FP32 pipe:
+// every node's four conserved components (and its split fluxes, and every
+// face's flux) sit together as one float4 in shared memory, so a stencil
+// read is one 128-bit shared load per node instead of four, and the index
+// arithmetic is done once per node.
+//
+// Shared memory (float4 elements unless noted):
+//   Us   [HI][HJ]          state tile + 3-node halo (FP32)
+//   Fp,Fm[HI][TJ] / [TI][HJ] split fluxes of the x / y sweep
+//   Hf   [TI+1][TJ] / [TI][TJ+1] face fluxes of the x / y sweep
+//   U64  double [4][TI][TJ] the tile's FP64 input values (kept from the load)
+//   Un64 double [4][TI][TJ] the tile's FP64 U^n (stages 2-3, cp.async)
+#pragma once
+
+#include "convert.cuh"
+#include "physics.cuh"
+
+namespace wenofd {
+namespace dev {
+
+template <int TI, int TJ>
+struct StageSmem32 {
+  static constexpr int HI = TI + 6, HJ = TJ + 6;
+  static constexpr int kU = HI * HJ;
+  static constexpr int kSplit = HI * TJ > TI * HJ ? HI * TJ : TI * HJ;
+  static constexpr int kFace = (TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1);
+  static constexpr int kKeep = 2 * 4 * TI * TJ;  // doubles
+  static constexpr size_t bytes = sizeof(float4) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
+};
+
+__device__ __forceinline__ float4 f4_split_store(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+// Pointwise Lax-Friedrichs split of one node (flux_split in physics.cuh).
+template <int DIR>
+__device__ __forceinline__ void split4(float gamma, const float4 q, float4 &fm, float4 &fp) {
+  const float U[4] = {q.x, q.y, q.z, q.w};
+  float m[4], p[4];
+  flux_split<float, DIR>(gamma, U, m, p);
+  fm = make_float4(m[0], m[1], m[2], m[3]);
+  fp = make_float4(p[0], p[1], p[2], p[3]);
+}
+
+// Linear fifth-order upwind flux of all four components (linear_upwind in
+// stage_kernel.cuh, same coefficients and order): P0..P4 = F+ at nodes
+// face-3..face+1, M0..M4 = F- at nodes face-2..face+2.
+__device__ __forceinline__ float lin5(float p0, float p1, float p2, float p3, float p4, float m0, float m1, float m2,
+                                      float m3, float m4) {
+  const float c0 = float(2.0 / 60.0), c1 = float(-13.0 / 60.0), c2 = float(47.0 / 60.0), c3 = float(27.0 / 60.0),
+              c4 = float(-3.0 / 60.0);
+  const float plus = c0 * p0 + c1 * p1 + c2 * p2 + c3 * p3 + c4 * p4;
+  const float minus = c0 * m4 + c1 * m3 + c2 * m2 + c3 * m1 + c4 * m0;
+  return plus + minus;
+}
+
+__device__ __forceinline__ float4 linear_face4(const float4 *P, const float4 *M, int ss) {
+  const float4 p0 = P[0], p1 = P[ss], p2 = P[2 * ss], p3 = P[3 * ss], p4 = P[4 * ss];
+  const float4 m0 = M[0], m1 = M[ss], m2 = M[2 * ss], m3 = M[3 * ss], m4 = M[4 * ss];
+  return make_float4(lin5(p0.x, p1.x, p2.x, p3.x, p4.x, m0.x, m1.x, m2.x, m3.x, m4.x),
+                     lin5(p0.y, p1.y, p2.y, p3.y, p4.y, m0.y, m1.y, m2.y, m3.y, m4.y),
+                     lin5(p0.z, p1.z, p2.z, p3.z, p4.z, m0.z, m1.z, m2.z, m3.z, m4.z),
+                     lin5(p0.w, p1.w, p2.w, p3.w, p4.w, m0.w, m1.w, m2.w, m3.w, m4.w));
+}
+
+// Characteristic WENO face from float4 stencils (face_flux_st).
+template <int DIR, int SCHEME>
+__device__ __forceinline__ float4 weno_face4(float gamma, float zpl, const float4 um4, const float4 u04,
+                                             const float4 *P, const float4 *M, int ss) {
+  const float um[4] = {um4.x, um4.y, um4.z, um4.w}, u0[4] = {u04.x, u04.y, u04.z, u04.w};
+  float out[4];
+  face_flux_st<float, DIR, SCHEME>(gamma, zpl, um, u0, Float4Stencil{P, ss}, Float4Stencil{M, ss}, out);
+  return make_float4(out[0], out[1], out[2], out[3]);
+}
+
+__device__ __forceinline__ void cp_async8_f32(void *smem, const void *gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all_f32() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One tile (TI x TJ interior nodes from i0, j0) of one RK stage, all NT
+// threads of the block.  ROUTE: faces take the linear upwind flux unless a
+// node of their stencil line is flagged (a.flags).  COH: inputs may have
+// been written earlier in the same launch by other blocks (persistent
+// batched kernel): loads through L2, U^n read in the epilogue.
+template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false>
+__device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a, const int i0, const int j0,
+                                               unsigned char *smem_raw) {
+  using S = StageSmem32<TI, TJ>;
+  constexpr int HI = S::HI, HJ = S::HJ;
+  float4 *Us = reinterpret_cast<float4 *>(smem_raw);
+  float4 *Fp = Us + S::kU;
+  float4 *Fm = Fp + S::kSplit;
+  float4 *Hf = Fm + S::kSplit;
+  double *U64 = reinterpret_cast<double *>(Hf + S::kFace);
+  double *Un64 = U64 + 4 * TI * TJ;
+  constexpr int FI = TI + 4, FJ = TJ + 4;
+  constexpr int kMaxFaces = S::kFace;
+  __shared__ unsigned char sflag[ROUTE ? FI * FJ : 1];
+  __shared__ short slist[ROUTE ? kMaxFaces : 1];
+  __shared__ int scount;
+
+  const float gamma = g.gamma32, zpl = g.zpl32;
+  const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
+
+  // stages 2 and 3: fetch this tile's U^n now, used only by the epilogue
+  if constexpr (!COH) {
+    if (a.mode == kModeRK && !stage1) {
+      for (int t = threadIdx.x; t < 4 * TI * TJ; t += NT) {
+        const int r = t / (TI * TJ), q = t - r * (TI * TJ);
+        const int i = q / TJ, j = q - (q / TJ) * TJ;
+        if (i0 + i < g.nx && j0 + j < g.ny)
+          cp_async8_f32(&Un64[t], &a.un[r * g.plane + (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j)]);
+      }
+    }
+  }
+
+  // --- state tile with halo, one node (four components) per thread and
+  // item: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).  All loads of a
+  // thread are issued before any is converted.
+  {
+    constexpr int NLD = (HI * HJ + NT - 1) / NT;
+    double v[NLD][4];
+#pragma unroll
+    for (int k = 0; k < NLD; ++k) {
+      const int t = threadIdx.x + k * NT;
+      const int hi = t / HJ, hj = t - (t / HJ) * HJ;
+      const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
+      const bool ok = t < HI * HJ && ei < g.nxt && ej < g.nyt;
+      const double *src = a.uin + (long long)ei * g.pitch + ej;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if constexpr (COH) v[k][r] = ok ? __ldcg(src + r * g.plane) : 0.0;
+        else v[k][r] = ok ? __ldg(src + r * g.plane) : 0.0;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NLD; ++k) {
+      const int t = threadIdx.x + k * NT;
+      if (t < HI * HJ) {
+        Us[t] = make_float4(f64_to_f32(v[k][0]), f64_to_f32(v[k][1]), f64_to_f32(v[k][2]), f64_to_f32(v[k][3]));
+        const int hi = t / HJ, hj = t - (t / HJ) * HJ;
+        if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
+          const int q = (hi - 3) * TJ + hj - 3;
+#pragma unroll
+          for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = v[k][r];
+        }
+      }
+    }
+  }
+  if constexpr (ROUTE) {
+    for (int t = threadIdx.x; t < FI * FJ; t += NT) {
+      const int fi = t / FJ, fj = t - (t / FJ) * FJ;
+      const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;  // nodes i0-2+fi, j0-2+fj
+      sflag[t] = (ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
+    }
+    if (threadIdx.x == 0) scount = 0;
+  }
+  __syncthreads();
+
+  // --- x sweep: split fluxes of halo rows 0..HI-1, tile columns
+  for (int t = threadIdx.x; t < HI * TJ; t += NT) {
+    const int hi = t / TJ, j = t - (t / TJ) * TJ;
+    split4<0>(gamma, Us[hi * HJ + j + 3], Fm[t], Fp[t]);
+  }
+  __syncthreads();
+  // x faces f = 0..TI between tile nodes f-1 and f: F+ rows f..f+4, F- rows f+1..f+5
+  for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
+    const int f = t / TJ, j = t - (t / TJ) * TJ;
+    if (i0 + f > g.nx || j0 + j >= g.ny) continue;
+    if constexpr (ROUTE) {
+      Hf[t] = linear_face4(Fp + t, Fm + t + TJ, TJ);
+      const unsigned char *fl = sflag + f * FJ + (j + 2);  // nodes f-2 .. f+1
+      if (fl[0] | fl[FJ] | fl[2 * FJ] | fl[3 * FJ]) slist[atomicAdd(&scount, 1)] = short(t);
+    } else {
+      Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
+                                    Fm + t + TJ, TJ);
+    }
+  }
+  if constexpr (ROUTE) {
+    __syncthreads();
+    const int nw = scount;
+    for (int q = threadIdx.x; q < nw; q += NT) {
+      const int t = slist[q];
+      const int f = t / TJ, j = t - (t / TJ) * TJ;
+      Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
+                                    Fm + t + TJ, TJ);
+    }
+  }
+  __syncthreads();
+
+  // x term of the node's RHS (rhs zeroed, then += in the x sweep)
+  constexpr int PPT = (TI * TJ + NT - 1) / NT;
+  float4 rhs[PPT];
+  const float idx = g.inv_dx32, idy = g.inv_dy32;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int t = threadIdx.x + k * NT;
+    if (t < TI * TJ) {
+      const float4 hr = Hf[t + TJ], hl = Hf[t];
+      rhs[k] = make_float4(-(hr.x - hl.x) * idx, -(hr.y - hl.y) * idx, -(hr.z - hl.z) * idx, -(hr.w - hl.w) * idx);
+    }
+  }
+  if constexpr (ROUTE) {
+    if (threadIdx.x == 0) scount = 0;
+  }
+  __syncthreads();
+
+  // --- y sweep: split fluxes of tile rows, halo columns 0..HJ-1
+  for (int t = threadIdx.x; t < TI * HJ; t += NT) {
+    const int i = t / HJ, hj = t - (t / HJ) * HJ;
+    split4<1>(gamma, Us[(i + 3) * HJ + hj], Fm[t], Fp[t]);
+  }
+  __syncthreads();
+  // y faces f = 0..TJ of row i: F+ columns f..f+4, F- columns f+1..f+5
+  for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
+    const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
+    if (i0 + i >= g.nx || j0 + f > g.ny) continue;
+    const int s = i * HJ + f;
+    if constexpr (ROUTE) {
+      Hf[t] = linear_face4(Fp + s, Fm + s + 1, 1);
+      const unsigned char *fl = sflag + (i + 2) * FJ + f;  // nodes f-2 .. f+1 along y
+      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount, 1)] = short(t);
+    } else {
+      Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,
+                                    Fm + s + 1, 1);
+    }
+  }
+  if constexpr (ROUTE) {
+    __syncthreads();
+    const int nw = scount;
+    for (int q = threadIdx.x; q < nw; q += NT) {
+      const int t = slist[q];
+      const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
+      const int s = i * HJ + f;
+      Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,
+                                    Fm + s + 1, 1);
+    }
+  }
+  __syncthreads();
+
+  // --- y term, source, RK combination in FP64, store
+  const double dt = COH ? __ldcg(a.dt) : *a.dt;
+  const double cdt = a.c * dt;
+  if constexpr (!COH) {
+    cp_async_wait_all_f32();
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int t = threadIdx.x + k * NT;
+    if (t >= TI * TJ) continue;
+    const int i = t / TJ, j = t - (t / TJ) * TJ;
+    if (i0 + i >= g.nx || j0 + j >= g.ny) continue;
+    const float4 hr = Hf[i * (TJ + 1) + j + 1], hl = Hf[i * (TJ + 1) + j];
+    float rr[4] = {rhs[k].x - (hr.x - hl.x) * idy, rhs[k].y - (hr.y - hl.y) * idy, rhs[k].z - (hr.z - hl.z) * idy,
+                   rhs[k].w - (hr.w - hl.w) * idy};
+    if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
+      const float4 q = Us[(i + 3) * HJ + j + 3];
+      rr[3] += q.z * 1.0f;
+      rr[2] += q.x * 1.0f;
+    }
+    const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const long long ix = r * g.plane + gidx;
+      const double rd = f32_to_f64(rr[r]);
+      const double ui = U64[r * TI * TJ + t];
+      if (a.mode == kModeRHS) a.uout[ix] = rd;
+      else if (stage1) a.uout[ix] = fma(cdt, rd, ui);  // a = 1, b = 0: one FMA
+      else if constexpr (COH) a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
+      else a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[r * TI * TJ + t]));
+    }
+  }
+}
+
+}  // namespace dev
+}  // namespace wenofd

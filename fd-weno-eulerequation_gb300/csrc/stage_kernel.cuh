@@ -19,6 +19,7 @@
 
 #include "convert.cuh"
 #include "physics.cuh"
+#include "stage_f32.cuh"
 
 namespace wenofd {
 namespace dev {
@@ -333,11 +334,21 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
 // characteristic-WENO path runs for a few percent of the faces, so trading
 // registers on that path for occupancy everywhere else pays.
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a) {
+__global__ void __launch_bounds__(NT, ROUTE && NT <= 256 ? 3 : 1) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // first interior node of the tile (0-based)
-  stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+  if constexpr (sizeof(T) == 4)
+    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+  else
+    stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+}
+
+// Dynamic shared memory of one stage tile.
+template <typename T, int TI, int TJ>
+constexpr size_t stage_smem_bytes() {
+  if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ>::bytes;
+  else return StageSmem<T, TI, TJ>::bytes;
 }
 
 // Host-side launcher for one precision: picks the kernel instance for the
@@ -345,7 +356,7 @@ __global__ void __launch_bounds__(NT, ROUTE ? 3 : 1) k_stage(Geom g, StageArgs a
 template <typename T, int TI, int NT, bool ROUTE = false>
 cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cudaStream_t s) {
   constexpr int TJ = 32;
-  using Sm = StageSmem<T, TI, TJ>;
+  constexpr size_t smem = stage_smem_bytes<T, TI, TJ>();
   const dim3 grid((g.ny + TJ - 1) / TJ, (g.nx + TI - 1) / TI);
   void (*fn)(Geom, StageArgs) = nullptr;
   switch (scheme) {
@@ -364,11 +375,11 @@ cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cud
   if (e != cudaSuccess) return e;
   const unsigned long long bit = 1ull << (dev & 63);
   if (!(configured[scheme & 3] & bit)) {
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Sm::bytes));
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
     configured[scheme & 3] |= bit;
   }
-  fn<<<grid, NT, Sm::bytes, s>>>(g, a);
+  fn<<<grid, NT, smem, s>>>(g, a);
   return cudaGetLastError();
 }
 
