@@ -37,7 +37,8 @@ CUDA_UNITS = {
     "stage_fp32.cu": [],
     "aux_kernels.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
-    "learned.cu": ["-fmad=false"],
+    "learned_data.cu": ["-fmad=false"],
+    "learned.cu": [],
     "batch_fp64.cu": ["-fmad=false"],
     "batch_fp32.cu": [],
 }

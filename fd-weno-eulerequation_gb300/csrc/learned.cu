@@ -2,19 +2,12 @@
 // sigmoid) that decides which faces need characteristic WENO-Z and which can
 // take the linear fifth-order upwind flux.  No counterpart in the reference;
 // WENO-Z (include/Utility.hpp:457-504) is both its label source and its
-// fallback.
+// fallback.  Its training data (features, labels) is learned_data.cu.
 //
-//  - k_features: 5x5 windows of density and pressure per cell, normalised
-//    (FP32), the network's 50 inputs;
-//  - k_labels: 1 where WENO-Z's nonlinear weights leave the linear weights
-//    (FP64, the training target);
 //  - k_mlp_forward / k_mlp_backward / k_adam: FP32 training kernels;
 //  - k_indicator_tc: inference on the 5th-generation tensor cores -- BF16
 //    operands in shared memory, tcgen05.mma with FP32 accumulators in tensor
-//    memory, tcgen05.ld for the epilogue -- writing one flag per cell.
-//
-// Compiled with -fmad=false: features and labels then round exactly like the
-// oracle's restatement (oracle/wenofd_oracle.c), which tests hold them to.
+//    memory, tcgen05.ld for the epilogues -- writing one flag per cell.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -23,161 +16,10 @@
 #include <vector>
 
 #include "../../include/wenofd.h"
-#include "convert.cuh"
-#include "physics.cuh"
-#include "wenofd_internal.h"
+#include "learned_common.cuh"
 
 namespace wenofd {
 namespace lrn {
-
-constexpr int kIn = 50, kHid = 32;
-constexpr int oW1 = 0, oB1 = 1600, oW2 = 1632, oB2 = 2656, oW3 = 2688, oB3 = 2720;
-constexpr int kParams = 2721;
-constexpr float kFlat = 1e-4f;  // relative range below which a window counts as flat
-
-__device__ __forceinline__ float gelu(float z) {
-  const float k = 0.7978845608028654f;  // sqrt(2/pi)
-  return 0.5f * z * (1.0f + tanhf(k * (z + 0.044715f * z * z * z)));
-}
-
-__device__ __forceinline__ float gelu_grad(float z) {
-  const float k = 0.7978845608028654f;
-  const float t = tanhf(k * (z + 0.044715f * z * z * z));
-  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * k * (1.0f + 3.0f * 0.044715f * z * z);
-}
-
-__device__ __forceinline__ float pressure32(float gamma, float r, float mu, float mv, float E) {
-  const float u = mu / r, v = mv / r;
-  return (gamma - 1.0f) * (E - 0.5f * r * (u * u + v * v));
-}
-
-// (v - centre) * (1 / max|v - centre|) over the 25-point window, or zeros when the
-// window is flat (range <= 1e-4 (|centre| + 1e-12)).
-__device__ __forceinline__ void normalise(const float w[25], float out[25]) {
-  const float c = w[12];
-  float R = 0.0f;
-#pragma unroll
-  for (int k = 0; k < 25; ++k) R = fmaxf(R, fabsf(w[k] - c));
-  if (R <= kFlat * (fabsf(c) + 1e-12f)) {
-#pragma unroll
-    for (int k = 0; k < 25; ++k) out[k] = 0.0f;
-    return;
-  }
-  const float inv = 1.0f / R;
-#pragma unroll
-  for (int k = 0; k < 25; ++k) out[k] = (w[k] - c) * inv;
-}
-
-// GELU for inference: the same tanh form with the hardware tanh
-// approximation (the BF16 operands that follow are coarser than its error).
-__device__ __forceinline__ float gelu_fast(float z) {
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.7978845608028654f * (z + 0.044715f * z * z * z)));
-  return 0.5f * z * (1.0f + t);
-}
-
-// ------------------------------------------------------------- features
-
-__global__ void k_features(Geom g, const double *U, float *feat) {
-  const long long n = (long long)g.nx * g.ny;
-  const float gam = float(g.gamma);
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-    const int i = int(c / g.ny), j = int(c - (c / g.ny) * g.ny);
-    float wr[25], wp[25];
-    for (int a = 0; a < 5; ++a)
-      for (int b = 0; b < 5; ++b) {
-        const long long base = (long long)(kGhost + i + a - 2) * g.pitch + (kGhost + j + b - 2);
-        const float r = float(U[base]), mu = float(U[g.plane + base]), mv = float(U[2 * g.plane + base]),
-                    E = float(U[3 * g.plane + base]);
-        wr[a * 5 + b] = r;
-        wp[a * 5 + b] = pressure32(gam, r, mu, mv, E);
-      }
-    float o[25];
-    normalise(wr, o);
-    for (int k = 0; k < 25; ++k) feat[c * kIn + k] = o[k];
-    normalise(wp, o);
-    for (int k = 0; k < 25; ++k) feat[c * kIn + 25 + k] = o[k];
-  }
-}
-
-// --------------------------------------------------------------- labels
-
-// Row k of the left eigenvectors (utils/equations.hpp:174-236) from the
-// face-average state's primitives.
-template <int DIR>
-__device__ __forceinline__ void left_row(int k, double u, double v, double c, double B1, double B2, double l[4]) {
-  const double ic = 1.0 / c, nc = (DIR == 0 ? u : v) / c;
-  if (DIR == 0) {
-    if (k == 0) { l[0] = (B2 + nc) / 2; l[1] = -(B1 * u + ic) / 2; l[2] = -(B1 * v) / 2; l[3] = B1 / 2; }
-    if (k == 1) { l[0] = v; l[1] = 0; l[2] = -1; l[3] = 0; }
-    if (k == 2) { l[0] = 1 - B2; l[1] = B1 * u; l[2] = B1 * v; l[3] = -B1; }
-    if (k == 3) { l[0] = (B2 - nc) / 2; l[1] = -(B1 * u - ic) / 2; l[2] = -B1 * v / 2; l[3] = B1 / 2; }
-  } else {
-    if (k == 0) { l[0] = (B2 + nc) / 2; l[1] = -(B1 * u) / 2; l[2] = -(B1 * v + ic) / 2; l[3] = B1 / 2; }
-    if (k == 1) { l[0] = -u; l[1] = 1; l[2] = 0; l[3] = 0; }
-    if (k == 2) { l[0] = 1 - B2; l[1] = B1 * u; l[2] = B1 * v; l[3] = -B1; }
-    if (k == 3) { l[0] = (B2 - nc) / 2; l[1] = -(B1 * u) / 2; l[2] = -(B1 * v - ic) / 2; l[3] = B1 / 2; }
-  }
-}
-
-__device__ double side_deviation(const double v[5], double scale) {
-  double lo = v[0], hi = v[0];
-  for (int s = 1; s < 5; ++s) {
-    lo = v[s] < lo ? v[s] : lo;
-    hi = v[s] > hi ? v[s] : hi;
-  }
-  if (hi - lo <= 1e-2 * scale) return 0.0;
-  double w0, w1, w2;
-  dev::wenoz_weights<double>(v[0], v[1], v[2], v[3], v[4], w0, w1, w2);
-  return fmax(fabs(w0 - 0.1), fmax(fabs(w1 - 0.6), fabs(w2 - 0.3)));
-}
-
-// Largest WENO-Z weight deviation over the characteristic fields and sides
-// of the face between (ei-1, ej) and (ei, ej) (DIR 0) or (ei, ej-1), (ei, ej).
-template <int DIR>
-__device__ double face_deviation(const Geom &g, const double *U, int ei, int ej) {
-  const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
-  double ave[4];
-  for (int r = 0; r < 4; ++r)
-    ave[r] = 0.5 * (U[r * g.plane + (long long)(ei - di) * g.pitch + (ej - dj)] +
-                    U[r * g.plane + (long long)ei * g.pitch + ej]);
-  double u, v, p;
-  dev::primitives<double>(g.gamma, ave, u, v, p);
-  const double c = sqrt(g.gamma * p / ave[0]);
-  const double B1 = (g.gamma - 1) / (c * c);
-  const double B2 = B1 * (u * u + v * v) / 2;
-  double fp[6][4], fm[6][4];
-  for (int s = 0; s < 6; ++s) {
-    double q[4];
-    for (int r = 0; r < 4; ++r) q[r] = U[r * g.plane + (long long)(ei + (s - 3) * di) * g.pitch + (ej + (s - 3) * dj)];
-    dev::flux_split<double, DIR>(g.gamma, q, fm[s], fp[s]);
-  }
-  double vp[4][5], vm[4][5], scale = 0.0;
-  for (int k = 0; k < 4; ++k) {
-    double l[4];
-    left_row<DIR>(k, u, v, c, B1, B2, l);
-    for (int s = 0; s < 5; ++s) {
-      vp[k][s] = l[0] * fp[s][0] + l[1] * fp[s][1] + l[2] * fp[s][2] + l[3] * fp[s][3];
-      vm[k][4 - s] = l[0] * fm[s + 1][0] + l[1] * fm[s + 1][1] + l[2] * fm[s + 1][2] + l[3] * fm[s + 1][3];
-      scale = fmax(scale, fmax(fabs(vp[k][s]), fabs(vm[k][4 - s])));
-    }
-  }
-  double dev = 0.0;
-  for (int k = 0; k < 4; ++k) dev = fmax(dev, fmax(side_deviation(vp[k], scale), side_deviation(vm[k], scale)));
-  return dev;
-}
-
-__global__ void k_labels(Geom g, const double *U, unsigned char *labels) {
-  const long long n = (long long)g.nx * g.ny;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
-    const int ei = kGhost + int(c / g.ny), ej = kGhost + int(c - (c / g.ny) * g.ny);
-    double d = face_deviation<0>(g, U, ei, ej);
-    d = fmax(d, face_deviation<0>(g, U, ei + 1, ej));
-    d = fmax(d, face_deviation<1>(g, U, ei, ej));
-    d = fmax(d, face_deviation<1>(g, U, ei, ej + 1));
-    labels[c] = d > 1e-2 ? 1 : 0;
-  }
-}
 
 // ---------------------------------------------------- FP32 training kernels
 
@@ -302,34 +144,39 @@ __global__ void k_adam(float *P, const float *G, float *M, float *V, int step, f
 //
 // One CTA of 128 threads runs tiles of 4 x 32 cells (x by y).  Per tile:
 //   1. density and pressure of the 8 x 36 node patch around the tile -> smem;
-//   2. each thread builds its cell's 50 features, writes them as BF16 into
-//      A1 [128 x 64] (K padded with zeros) in the no-swizzle K-major layout:
-//      8-row x 16-byte core matrices, K-adjacent cores 128 B apart (LBO),
-//      8-row groups KC*128 B apart (SBO);
+//   2. each thread builds its cell's 50 features and writes them as BF16
+//      into A1 [128 x 64]: columns 50 and 51 hold 1.0 so that the bias of
+//      layer 1 (split into a BF16 high and low part, columns 50 and 51 of
+//      W1) is added by the tensor core; the rest is zero padding.  Operands
+//      use the no-swizzle K-major layout: 8-row x 16-byte core matrices,
+//      K-adjacent cores 128 B apart (LBO), 8-row groups KC*128 B apart (SBO);
 //   3. one thread issues 4 x tcgen05.mma (M=128, N=32, K=16, BF16 in, FP32
-//      accumulate) D1 = A1 * W1^T into tensor memory columns [0, 32);
-//   4. each warp reads its 32 rows back (tcgen05.ld 32x32b.x32), adds b1,
-//      applies GELU, writes BF16 A2 [128 x 32];
-//   5. 2 x tcgen05.mma D2 = A2 * W2^T into columns [32, 64);
-//   6. read back, GELU, the 32 -> 1 layer on the CUDA cores, threshold ->
-//      flag.
+//      accumulate): D1 = A1 * W1^T into tensor-memory columns [0, 32);
+//   4. each warp reads its 32 rows back (tcgen05.ld 32x32b.x32), applies
+//      GELU in packed BF16 pairs and writes A2 [128 x 48] (columns 32 and 33
+//      are 1.0 for the bias of layer 2, the rest zero);
+//   5. 3 x tcgen05.mma: D2 = A2 * W2^T into columns [32, 64);
+//   6. read back, GELU, write the activations over A2;
+//   7. 3 x tcgen05.mma (N = 16): D3 = A2 * W3^T into columns [0, 16), with
+//      W3 row 0 = the output weights' BF16 high parts (and b3), row 1 their
+//      low parts; logit = D3[0] + D3[1], compared with the threshold.
 // MMA completion is signalled through an mbarrier (tcgen05.commit); every
 // wait on it is bounded and on give-up the kernel records an error and
 // stops issuing work, then releases its tensor memory.
 
 constexpr int kTileI = 4, kTileJ = 32, kCells = kTileI * kTileJ;  // 128 = MMA M
 constexpr int kPI = kTileI + 4, kPJ = kTileJ + 4;                   // node patch
-constexpr int kK1 = 64, kK2 = 32;
+constexpr int kK1 = 64, kK2 = 48, kN3 = 16;
 constexpr unsigned kWaitLimit = 1u << 22;
 
-struct IndicatorWeights {       // device buffer prepared by the host
-  __nv_bfloat16 w1[kHid * kK1];  // canonical no-swizzle K-major layout
-  __nv_bfloat16 w2[kHid * kK2];
-  float b1[kHid], b2[kHid], w3[kHid], b3;
+struct IndicatorWeights {  // device buffer prepared by the host (BF16, canonical layout)
+  __nv_bfloat16 w1[kHid * kK1];  // [32 x 64]: W1 | b1 hi | b1 lo | 0
+  __nv_bfloat16 w2[kHid * kK2];  // [32 x 48]: W2 | b2 hi | b2 lo | 0
+  __nv_bfloat16 w3[kN3 * kK2];   // [16 x 48]: row 0 w3 hi | b3 hi | b3 lo, row 1 w3 lo, rest 0
 };
 
 // element (row, k) of a K-major operand with KC = K/8 core columns
-__device__ __forceinline__ int canon_off(int row, int k, int kc) {
+__host__ __device__ __forceinline__ int canon_off(int row, int k, int kc) {
   return ((row >> 3) * kc + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7);  // in elements (2 bytes)
 }
 
@@ -357,6 +204,17 @@ __device__ __forceinline__ void mma_bf16(unsigned tmem_d, unsigned long long a, 
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// D[tmem_d] = A[128 x K] * B[N x K]^T, K a multiple of 16, both operands in
+// the canonical layout with K/8 core columns.
+template <int K, int N>
+__device__ __forceinline__ void mma_layer(unsigned tmem_d, const void *A, const void *B) {
+  const unsigned a0 = smem_u32(A), b0 = smem_u32(B);
+#pragma unroll
+  for (int kk = 0; kk < K / 16; ++kk)
+    mma_bf16(tmem_d, mdesc(a0 + kk * 256, 128, (K / 8) * 128), mdesc(b0 + kk * 256, 128, (K / 8) * 128),
+             idesc_bf16(128, N), kk > 0);
 }
 
 __device__ __forceinline__ void mma_commit(unsigned mbar) {
@@ -392,9 +250,50 @@ __device__ __forceinline__ void tmem_ld32(unsigned taddr, float v[32]) {
   for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+__device__ __forceinline__ void tmem_ld2(unsigned taddr, float v[2]) {
+  unsigned r0, r1;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];" : "=r"(r0), "=r"(r1) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  v[0] = __uint_as_float(r0);
+  v[1] = __uint_as_float(r1);
+}
+
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned bf2_bits(__nv_bfloat162 v) { return *reinterpret_cast<unsigned *>(&v); }
+__device__ __forceinline__ __nv_bfloat162 bits_bf2(unsigned u) { return *reinterpret_cast<__nv_bfloat162 *>(&u); }
+
+// GELU (tanh form) of two pre-activations in packed BF16 arithmetic with the
+// hardware tanh: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).  The
+// result is the next layer's BF16 operand, so BF16 intermediates lose
+// nothing that the operand rounding keeps.
+__device__ __forceinline__ unsigned gelu_bf16x2(float z0, float z1) {
+  const __nv_bfloat162 z = __floats2bfloat162_rn(z0, z1);
+  const __nv_bfloat162 k1 = __float2bfloat162_rn(0.7978845608028654f);
+  const __nv_bfloat162 k3 = __float2bfloat162_rn(0.7978845608028654f * 0.044715f);
+  const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
+  const __nv_bfloat162 u = __hmul2(z, __hfma2(__hmul2(z, z), k3, k1));
+  unsigned t;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(bf2_bits(u)));
+  const __nv_bfloat162 h = __hmul2(z, half);
+  return bf2_bits(__hfma2(h, bits_bf2(t), h));
+}
+
+// GELU of the 32 accumulator columns of this thread's row into 4 x 16-byte
+// chunks (columns 0..31) of a canonical-layout operand with KC core columns.
+__device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row, int kc) {
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    uint4 q;
+    q.x = gelu_bf16x2(z[8 * c + 0], z[8 * c + 1]);
+    q.y = gelu_bf16x2(z[8 * c + 2], z[8 * c + 3]);
+    q.z = gelu_bf16x2(z[8 * c + 4], z[8 * c + 5]);
+    q.w = gelu_bf16x2(z[8 * c + 6], z[8 * c + 7]);
+    *reinterpret_cast<uint4 *>(&A[canon_off(row, 8 * c, kc)]) = q;
+  }
+}
 
 __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
                                                          float logit_threshold, unsigned char *flags, int flag_pitch,
@@ -404,24 +303,21 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
   __shared__ __align__(128) __nv_bfloat16 sA2[kCells * kK2];
   __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
   __shared__ __align__(128) __nv_bfloat16 sB2[kHid * kK2];
+  __shared__ __align__(128) __nv_bfloat16 sB3[kN3 * kK2];
   __shared__ float sRho[kPI * kPJ], sPre[kPI * kPJ];
-  __shared__ float sb1[kHid], sb2[kHid], sw3[kHid];
-  __shared__ float sb3;
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ unsigned tmem_base_sh;
-  __shared__ int abort_sh;
 
   const int tid = threadIdx.x, warp = tid >> 5;
   for (int k = tid; k < kHid * kK1; k += kCells) sB1[k] = W->w1[k];
   for (int k = tid; k < kHid * kK2; k += kCells) sB2[k] = W->w2[k];
-  if (tid < kHid) {
-    sb1[tid] = W->b1[tid];
-    sb2[tid] = W->b2[tid];
-    sw3[tid] = W->w3[tid];
+  for (int k = tid; k < kN3 * kK2; k += kCells) sB3[k] = W->w3[k];
+  {  // constant columns 32..47 of this thread's row of A2: 1, 1, 0, ...
+    const unsigned one2 = 0x3F803F80u;  // two BF16 1.0
+    *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 32, kK2 / 8)]) = make_uint4(one2, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 40, kK2 / 8)]) = make_uint4(0u, 0u, 0u, 0u);
   }
   if (tid == 0) {
-    sb3 = W->b3;
-    abort_sh = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -441,24 +337,63 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
   const int ntiles = ((g.nx + kTileI - 1) / kTileI) * tiles_j;
   unsigned parity = 0;
 
+  // One layer: barrier (the operand writes are visible to the tensor core),
+  // MMA issue by thread 0, completion wait by every thread.  A wait that
+  // gives up marks this thread failed; the next barrier (a vote) turns that
+  // into a uniform stop of the whole CTA.
+  bool failed = false;
+  auto layer = [&](auto issue) -> bool {
+    fence_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(failed)) return false;
+    if (tid == 0) {
+      tc_fence_after();
+      issue();
+      mma_commit(mb);
+    }
+    if (!mbar_wait(mb, parity)) {
+      failed = true;
+      atomicExch(error, 1);
+    }
+    parity ^= 1u;
+    tc_fence_after();
+    return true;
+  };
+
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int i0 = (tile / tiles_j) * kTileI, j0 = (tile % tiles_j) * kTileJ;
-    // 1. node patch: nodes (i0-2 .. i0+5, j0-2 .. j0+33) of the interior index space
-    for (int k = tid; k < kPI * kPJ; k += kCells) {
-      const int pi = k / kPJ, pj = k - (k / kPJ) * kPJ;
-      const int ei = kGhost + i0 - 2 + pi, ej = kGhost + j0 - 2 + pj;
-      float r = 1.0f, p = 1.0f;
-      if (ei < g.nxt && ej < g.nyt) {
-        const long long b = (long long)ei * g.pitch + ej;
-        r = dev::f64_to_f32(U[b]);
-        p = pressure32(gam, r, dev::f64_to_f32(U[g.plane + b]), dev::f64_to_f32(U[2 * g.plane + b]),
-                       dev::f64_to_f32(U[3 * g.plane + b]));
+    // 1. node patch: nodes (i0-2 .. i0+5, j0-2 .. j0+33) of the interior index
+    // space; every load of a thread is issued before any is used
+    {
+      constexpr int NP = (kPI * kPJ + kCells - 1) / kCells;
+      double v[NP][4];
+      bool ok[NP];
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int k = tid + q * kCells;
+        const int pi = k / kPJ, pj = k - (k / kPJ) * kPJ;
+        const int ei = kGhost + i0 - 2 + pi, ej = kGhost + j0 - 2 + pj;
+        ok[q] = k < kPI * kPJ && ei < g.nxt && ej < g.nyt;
+        const double *src = U + (long long)ei * g.pitch + ej;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[q][r] = ok[q] ? __ldg(src + r * g.plane) : 0.0;
       }
-      sRho[k] = r;
-      sPre[k] = p;
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int k = tid + q * kCells;
+        if (k < kPI * kPJ) {
+          float r = 1.0f, p = 1.0f;
+          if (ok[q]) {
+            r = dev::f64_to_f32(v[q][0]);
+            p = pressure32(gam, r, dev::f64_to_f32(v[q][1]), dev::f64_to_f32(v[q][2]), dev::f64_to_f32(v[q][3]));
+          }
+          sRho[k] = r;
+          sPre[k] = p;
+        }
+      }
     }
     __syncthreads();
-    // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1
+    // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1; columns 50, 51 = 1
     {
       const int ci = warp, cj = tid & 31;
       float f[kK1];
@@ -473,102 +408,52 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
 #pragma unroll
         for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[(ci + a) * kPJ + cj + b];
       normalise(w, f + 25);
+      f[50] = 1.0f;
+      f[51] = 1.0f;
 #pragma unroll
-      for (int k = 50; k < kK1; ++k) f[k] = 0.0f;
+      for (int k = 52; k < kK1; ++k) f[k] = 0.0f;
 #pragma unroll
       for (int c = 0; c < kK1 / 8; ++c) {
         uint4 q;
-        __nv_bfloat162 h0 = __floats2bfloat162_rn(f[8 * c + 0], f[8 * c + 1]);
-        __nv_bfloat162 h1 = __floats2bfloat162_rn(f[8 * c + 2], f[8 * c + 3]);
-        __nv_bfloat162 h2 = __floats2bfloat162_rn(f[8 * c + 4], f[8 * c + 5]);
-        __nv_bfloat162 h3 = __floats2bfloat162_rn(f[8 * c + 6], f[8 * c + 7]);
-        q.x = *reinterpret_cast<unsigned *>(&h0);
-        q.y = *reinterpret_cast<unsigned *>(&h1);
-        q.z = *reinterpret_cast<unsigned *>(&h2);
-        q.w = *reinterpret_cast<unsigned *>(&h3);
+        q.x = bf2_bits(__floats2bfloat162_rn(f[8 * c + 0], f[8 * c + 1]));
+        q.y = bf2_bits(__floats2bfloat162_rn(f[8 * c + 2], f[8 * c + 3]));
+        q.z = bf2_bits(__floats2bfloat162_rn(f[8 * c + 4], f[8 * c + 5]));
+        q.w = bf2_bits(__floats2bfloat162_rn(f[8 * c + 6], f[8 * c + 7]));
         *reinterpret_cast<uint4 *>(&sA1[canon_off(tid, 8 * c, kK1 / 8)]) = q;
       }
     }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    // 3. layer 1 on the tensor cores
-    if (tid == 0 && !abort_sh) {
-      tc_fence_after();
-      const unsigned a0 = smem_u32(sA1), b0 = smem_u32(sB1);
-#pragma unroll
-      for (int kk = 0; kk < kK1 / 16; ++kk)
-        mma_bf16(tmem, mdesc(a0 + kk * 256, 128, (kK1 / 8) * 128), mdesc(b0 + kk * 256, 128, (kK1 / 8) * 128),
-                 idesc_bf16(128, 32), kk > 0);
-      mma_commit(mb);
-    }
-    if (!mbar_wait(mb, parity)) {
-      atomicExch(error, 1);
-      abort_sh = 1;
-    }
-    parity ^= 1u;
-    tc_fence_after();
-    // 4. epilogue 1
+    // 3. layer 1 (bias included)
+    if (!layer([&] { mma_layer<kK1, kHid>(tmem, sA1, sB1); })) break;
+    // 4. GELU -> A2
     {
       float z[32];
       tmem_ld32(tmem + lane_base, z);
-#pragma unroll
-      for (int c = 0; c < kK2 / 8; ++c) {
-        uint4 q;
-        unsigned *qq = reinterpret_cast<unsigned *>(&q);
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-          const int o = 8 * c + 2 * h;
-          __nv_bfloat162 v = __floats2bfloat162_rn(gelu_fast(z[o] + sb1[o]), gelu_fast(z[o + 1] + sb1[o + 1]));
-          qq[h] = *reinterpret_cast<unsigned *>(&v);
-        }
-        *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 8 * c, kK2 / 8)]) = q;
-      }
+      gelu_row_store(z, sA2, tid, kK2 / 8);
     }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    if (abort_sh) break;
     // 5. layer 2
-    if (tid == 0) {
-      tc_fence_after();
-      const unsigned a0 = smem_u32(sA2), b0 = smem_u32(sB2);
-#pragma unroll
-      for (int kk = 0; kk < kK2 / 16; ++kk)
-        mma_bf16(tmem + 32, mdesc(a0 + kk * 256, 128, (kK2 / 8) * 128), mdesc(b0 + kk * 256, 128, (kK2 / 8) * 128),
-                 idesc_bf16(128, 32), kk > 0);
-      mma_commit(mb);
-    }
-    if (!mbar_wait(mb, parity)) {
-      atomicExch(error, 1);
-      abort_sh = 1;
-    }
-    parity ^= 1u;
-    tc_fence_after();
-    // 6. epilogue 2 and the output layer
+    if (!layer([&] { mma_layer<kK2, kHid>(tmem + 32, sA2, sB2); })) break;
+    // 6. GELU -> A2 (layer 2 has read it)
     {
       float z[32];
       tmem_ld32(tmem + lane_base + 32, z);
-      float logit = sb3;
-#pragma unroll
-      for (int o = 0; o < kHid; ++o) logit += sw3[o] * gelu_fast(z[o] + sb2[o]);
+      gelu_row_store(z, sA2, tid, kK2 / 8);
+    }
+    // 7. output layer on the tensor cores, into the columns of D1
+    if (!layer([&] { mma_layer<kK2, kN3>(tmem, sA2, sB3); })) break;
+    {
+      float d[2];
+      tmem_ld2(tmem + lane_base, d);
+      const float logit = d[0] + d[1];
       const int i = i0 + warp, j = j0 + (tid & 31);
-      if (i < g.nx && j < g.ny && !abort_sh)
+      if (i < g.nx && j < g.ny && !failed)
         flags[(long long)(kGhost + i) * flag_pitch + (kGhost + j)] = logit > logit_threshold ? 1 : 0;
     }
     tc_fence_before();
-    __syncthreads();
-    if (abort_sh) break;
+    if (__syncthreads_or(failed)) break;
   }
   tc_fence_after();
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
-}
-
-int grid_for(long long work, int threads, int cap) {
-  long long b = (work + threads - 1) / threads;
-  if (b > cap) b = cap;
-  return int(b < 1 ? 1 : b);
 }
 
 }  // namespace lrn
@@ -586,36 +471,37 @@ static unsigned short bf16_rne(float f) {
 }
 
 void pack_indicator_weights(const float *params, void *host_out) {
-  lrn::IndicatorWeights *w = static_cast<lrn::IndicatorWeights *>(host_out);
+  using namespace lrn;
+  IndicatorWeights *w = static_cast<IndicatorWeights *>(host_out);
   std::memset(w, 0, sizeof(*w));
-  auto canon = [](int row, int k, int kc) { return ((row >> 3) * kc + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7); };
-  for (int o = 0; o < lrn::kHid; ++o)
-    for (int k = 0; k < lrn::kK1; ++k) {
-      const float v = k < lrn::kIn ? params[lrn::oW1 + o * lrn::kIn + k] : 0.0f;
-      const unsigned short b = bf16_rne(v);
-      std::memcpy(&w->w1[canon(o, k, lrn::kK1 / 8)], &b, 2);
-    }
-  for (int o = 0; o < lrn::kHid; ++o)
-    for (int k = 0; k < lrn::kK2; ++k) {
-      const unsigned short b = bf16_rne(params[lrn::oW2 + o * lrn::kHid + k]);
-      std::memcpy(&w->w2[canon(o, k, lrn::kK2 / 8)], &b, 2);
-    }
-  for (int o = 0; o < lrn::kHid; ++o) {
-    w->b1[o] = params[lrn::oB1 + o];
-    w->b2[o] = params[lrn::oB2 + o];
-    w->w3[o] = params[lrn::oW3 + o];
+  auto put = [](__nv_bfloat16 *M, int row, int k, int kc, float v) {
+    const unsigned short b = bf16_rne(v);
+    std::memcpy(&M[canon_off(row, k, kc)], &b, 2);
+  };
+  // v = hi + lo with hi, lo in BF16 (about 16 significant bits together)
+  auto hi_lo = [](float v, float &hi, float &lo) {
+    const unsigned short h = bf16_rne(v);
+    const unsigned u = unsigned(h) << 16;
+    std::memcpy(&hi, &u, 4);
+    lo = v - hi;
+  };
+  float hi, lo;
+  for (int o = 0; o < kHid; ++o) {
+    for (int k = 0; k < kIn; ++k) put(w->w1, o, k, kK1 / 8, params[oW1 + o * kIn + k]);
+    hi_lo(params[oB1 + o], hi, lo);
+    put(w->w1, o, kIn, kK1 / 8, hi);
+    put(w->w1, o, kIn + 1, kK1 / 8, lo);
+    for (int k = 0; k < kHid; ++k) put(w->w2, o, k, kK2 / 8, params[oW2 + o * kHid + k]);
+    hi_lo(params[oB2 + o], hi, lo);
+    put(w->w2, o, kHid, kK2 / 8, hi);
+    put(w->w2, o, kHid + 1, kK2 / 8, lo);
+    hi_lo(params[oW3 + o], hi, lo);
+    put(w->w3, 0, o, kK2 / 8, hi);
+    put(w->w3, 1, o, kK2 / 8, lo);
   }
-  w->b3 = params[lrn::oB3];
-}
-
-cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStream_t s) {
-  lrn::k_features<<<lrn::grid_for((long long)g.nx * g.ny, 128, 152 * 32), 128, 0, s>>>(g, U, feat);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, cudaStream_t s) {
-  lrn::k_labels<<<lrn::grid_for((long long)g.nx * g.ny, 128, 152 * 32), 128, 0, s>>>(g, U, labels);
-  return cudaGetLastError();
+  hi_lo(params[oB3], hi, lo);
+  put(w->w3, 0, kHid, kK2 / 8, hi);
+  put(w->w3, 0, kHid + 1, kK2 / 8, lo);
 }
 
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,

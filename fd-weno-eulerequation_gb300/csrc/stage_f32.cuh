@@ -73,6 +73,86 @@ __device__ __forceinline__ float4 weno_face4(float gamma, float zpl, const float
   return make_float4(out[0], out[1], out[2], out[3]);
 }
 
+// One characteristic field of a WENO face, for the routed form where the
+// faces that need WENO are few and would otherwise keep a handful of threads
+// busy while the block waits: four consecutive lanes take one face, lane k
+// projects the ten stencil fluxes on left eigenvector k and reconstructs
+// characteristic field k (face_flux_st's per-field work, same operation
+// order), the four fields are exchanged by shuffles, and lane k returns
+// component k of R * vh.  All 32 lanes of the warp must call it.
+template <int DIR, int SCHEME>
+__device__ __forceinline__ float weno_face_lane(float gamma, float zpl, const float4 um4, const float4 u04,
+                                                const float4 *P, const float4 *M, int ss, int k) {
+  const float um[4] = {um4.x, um4.y, um4.z, um4.w}, u0[4] = {u04.x, u04.y, u04.z, u04.w};
+  float ave[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) ave[r] = 0.5f * (um[r] + u0[r]);
+  float u, v, p;
+  primitives(gamma, ave, u, v, p);
+  const float rho = ave[0], E = ave[3];
+  const float c = tsqrt(tdiv(gamma * p, rho));
+  const float B1 = tdiv((gamma - 1.0f), (c * c));
+  const float B2 = B1 * (u * u + v * v) * 0.5f;
+  const float H = tdiv((E + p), rho);
+  const float ic = tdiv(1.0f, c);
+  const float nc = tdiv(DIR == 0 ? u : v, c);
+  const float B1u = B1 * u, B1v = B1 * v;
+  // row k of the left eigenvector matrix (face_flux_st)
+  float l0, l1, l2, l3;
+  if (DIR == 0) {
+    l0 = k == 0 ? (B2 + nc) * 0.5f : (k == 1 ? v : (k == 2 ? (1.0f - B2) : (B2 - nc) * 0.5f));
+    l1 = k == 0 ? -(B1u + ic) * 0.5f : (k == 1 ? 0.0f : (k == 2 ? B1u : -(B1u - ic) * 0.5f));
+    l2 = k == 0 ? -(B1v) * 0.5f : (k == 1 ? -1.0f : (k == 2 ? B1v : -B1v * 0.5f));
+    l3 = k == 0 ? B1 * 0.5f : (k == 1 ? 0.0f : (k == 2 ? -B1 : B1 * 0.5f));
+  } else {
+    l0 = k == 0 ? (B2 + nc) * 0.5f : (k == 1 ? -u : (k == 2 ? 1.0f - B2 : (B2 - nc) * 0.5f));
+    l1 = k == 0 ? -(B1u) * 0.5f : (k == 1 ? 1.0f : (k == 2 ? B1u : -(B1u) * 0.5f));
+    l2 = k == 0 ? -(B1v + ic) * 0.5f : (k == 1 ? 0.0f : (k == 2 ? B1v : -(B1v - ic) * 0.5f));
+    l3 = k == 0 ? B1 * 0.5f : (k == 1 ? 0.0f : (k == 2 ? -B1 : B1 * 0.5f));
+  }
+  float vp[5], vm[5];
+#pragma unroll
+  for (int s = 0; s < 5; ++s) {
+    const float4 a = P[s * ss], b = M[s * ss];
+    float x = l0 * a.x;
+    x += l1 * a.y;
+    x += l2 * a.z;
+    x += l3 * a.w;
+    vp[s] = x;
+    float y = l0 * b.x;
+    y += l1 * b.y;
+    y += l2 * b.z;
+    y += l3 * b.w;
+    vm[s] = y;
+  }
+  const float vhk = weno<float, SCHEME>(vp[0], vp[1], vp[2], vp[3], vp[4], zpl) +
+                    weno<float, SCHEME>(vm[4], vm[3], vm[2], vm[1], vm[0], zpl);
+  const int base = (threadIdx.x & 31) & ~3;
+  const float vh0 = __shfl_sync(0xffffffffu, vhk, base + 0);
+  const float vh1 = __shfl_sync(0xffffffffu, vhk, base + 1);
+  const float vh2 = __shfl_sync(0xffffffffu, vhk, base + 2);
+  const float vh3 = __shfl_sync(0xffffffffu, vhk, base + 3);
+  // row k of R (face_flux_st, utils/equations.hpp:239-299)
+  const float q2 = (u * u + v * v) * 0.5f;
+  float r0, r1, r2, r3;
+  if (DIR == 0) {
+    r1 = k == 0 ? 0.0f : (k == 1 ? 0.0f : (k == 2 ? -1.0f : -v));
+    r2 = k == 0 ? 1.0f : (k == 1 ? u : (k == 2 ? v : q2));
+    r3 = k == 0 ? 1.0f : (k == 1 ? u + c : (k == 2 ? v : H + c * u));
+    r0 = k == 0 ? 1.0f : (k == 1 ? u - c : (k == 2 ? v : H - c * u));
+  } else {
+    r1 = k == 0 ? 0.0f : (k == 1 ? 1.0f : (k == 2 ? 0.0f : u));
+    r2 = k == 0 ? 1.0f : (k == 1 ? u : (k == 2 ? v : q2));
+    r3 = k == 0 ? 1.0f : (k == 1 ? u : (k == 2 ? v + c : H + c * v));
+    r0 = k == 0 ? 1.0f : (k == 1 ? u : (k == 2 ? v - c : H - c * v));
+  }
+  float f = r0 * vh0;
+  f += r1 * vh1;
+  f += r2 * vh2;
+  f += r3 * vh3;
+  return f;
+}
+
 __device__ __forceinline__ void cp_async8_f32(void *smem, const void *gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
                "l"(gmem)
@@ -119,10 +199,14 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
 
   // --- state tile with halo, one node (four components) per thread and
   // item: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).  All loads of a
-  // thread are issued before any is converted.
+  // thread (state, and the routed form's node flags: tile + 2-node halo,
+  // flag node (fi, fj) = global (2 + i0 + fi, 2 + j0 + fj)) are issued
+  // before any is used.
   {
     constexpr int NLD = (HI * HJ + NT - 1) / NT;
+    constexpr int NFL = ROUTE ? (FI * FJ + NT - 1) / NT : 1;
     double v[NLD][4];
+    unsigned char fv[NFL];
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
@@ -134,6 +218,15 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       for (int r = 0; r < 4; ++r) {
         if constexpr (COH) v[k][r] = ok ? __ldcg(src + r * g.plane) : 0.0;
         else v[k][r] = ok ? __ldg(src + r * g.plane) : 0.0;
+      }
+    }
+    if constexpr (ROUTE) {
+#pragma unroll
+      for (int k = 0; k < NFL; ++k) {
+        const int t = threadIdx.x + k * NT;
+        const int fi = t / FJ, fj = t - (t / FJ) * FJ;
+        const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;
+        fv[k] = (t < FI * FJ && ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
       }
     }
 #pragma unroll
@@ -149,14 +242,14 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
         }
       }
     }
-  }
-  if constexpr (ROUTE) {
-    for (int t = threadIdx.x; t < FI * FJ; t += NT) {
-      const int fi = t / FJ, fj = t - (t / FJ) * FJ;
-      const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;  // nodes i0-2+fi, j0-2+fj
-      sflag[t] = (ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
+    if constexpr (ROUTE) {
+#pragma unroll
+      for (int k = 0; k < NFL; ++k) {
+        const int t = threadIdx.x + k * NT;
+        if (t < FI * FJ) sflag[t] = fv[k];
+      }
+      if (threadIdx.x == 0) scount = 0;
     }
-    if (threadIdx.x == 0) scount = 0;
   }
   __syncthreads();
 
@@ -182,11 +275,13 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   if constexpr (ROUTE) {
     __syncthreads();
     const int nw = scount;
-    for (int q = threadIdx.x; q < nw; q += NT) {
-      const int t = slist[q];
+    for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {  // 4 lanes per face, whole warps
+      const int q4 = base + (threadIdx.x & 31);
+      const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
       const int f = t / TJ, j = t - (t / TJ) * TJ;
-      Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
-                                    Fm + t + TJ, TJ);
+      const float o = weno_face_lane<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3],
+                                                Fp + t, Fm + t + TJ, TJ, q4 & 3);
+      if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
     }
   }
   __syncthreads();
@@ -231,12 +326,14 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   if constexpr (ROUTE) {
     __syncthreads();
     const int nw = scount;
-    for (int q = threadIdx.x; q < nw; q += NT) {
-      const int t = slist[q];
+    for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {
+      const int q4 = base + (threadIdx.x & 31);
+      const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
       const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
       const int s = i * HJ + f;
-      Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,
-                                    Fm + s + 1, 1);
+      const float o = weno_face_lane<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3],
+                                                Fp + s, Fm + s + 1, 1, q4 & 3);
+      if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
     }
   }
   __syncthreads();
