@@ -121,13 +121,15 @@ __device__ __forceinline__ double exact_speed(const Geom &g, double rho, double 
 // a non-positive or non-finite FP32 pressure get e = inf.
 __device__ __forceinline__ void screen_speed(const Geom &g, double rho_d, double mu_d, double mv_d, double E_d,
                                              float &s, float &e) {
+  // Explicit round-to-nearest operations: no multiply-add contraction, so
+  // every translation unit (the stage kernels' fused screen, the reduction
+  // kernels, the batched kernel) computes the same s and e.
   const float eps = 1.1920929e-07f;
-  const float r = f64_to_f32(rho_d), mu = f64_to_f32(mu_d), mv = f64_to_f32(mv_d),
-              E = f64_to_f32(E_d);
+  const float r = f64_to_f32(rho_d), mu = f64_to_f32(mu_d), mv = f64_to_f32(mv_d), E = f64_to_f32(E_d);
   const float u = __fdividef(mu, r), v = __fdividef(mv, r);
-  const float ke = 0.5f * r * (u * u + v * v);
-  const float pp = E - ke;
-  const float c2 = __fdividef(g.gamma32 * ((g.gamma32 - 1.0f) * pp), r);
+  const float ke = __fmul_rn(__fmul_rn(0.5f, r), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)));
+  const float pp = __fsub_rn(E, ke);
+  const float c2 = __fdividef(__fmul_rn(g.gamma32, __fmul_rn(__fsub_rn(g.gamma32, 1.0f), pp)), r);
   if (!(pp > 0.0f) || !(c2 > 0.0f) || !(c2 < 3.0e38f) || !(fabsf(u) < 3.0e38f) || !(fabsf(v) < 3.0e38f)) {
     s = 0.0f;
     e = __int_as_float(0x7f800000);
@@ -135,11 +137,14 @@ __device__ __forceinline__ void screen_speed(const Geom &g, double rho_d, double
   }
   const float c = sqrtf(c2);
   const float au = fabsf(u), av = fabsf(v);
-  s = (au + c) * g.inv_dx32 + (av + c) * g.inv_dy32;
-  const float rp = 12.0f * eps * (fabsf(E) + ke) / pp;
-  const float rc = 0.5f * rp + 2.0f * eps;
-  const float ex = au * 3.0f * eps + c * rc, ey = av * 3.0f * eps + c * rc;
-  e = 4.0f * ((ex * g.inv_dx32 + ey * g.inv_dy32) + s * 4.0f * eps) + 1e-12f * s;
+  s = __fadd_rn(__fmul_rn(__fadd_rn(au, c), g.inv_dx32), __fmul_rn(__fadd_rn(av, c), g.inv_dy32));
+  const float rp = __fdiv_rn(__fmul_rn(__fmul_rn(12.0f, eps), __fadd_rn(fabsf(E), ke)), pp);
+  const float rc = __fadd_rn(__fmul_rn(0.5f, rp), __fmul_rn(2.0f, eps));
+  const float ex = __fadd_rn(__fmul_rn(__fmul_rn(au, 3.0f), eps), __fmul_rn(c, rc));
+  const float ey = __fadd_rn(__fmul_rn(__fmul_rn(av, 3.0f), eps), __fmul_rn(c, rc));
+  e = __fadd_rn(__fmul_rn(4.0f, __fadd_rn(__fadd_rn(__fmul_rn(ex, g.inv_dx32), __fmul_rn(ey, g.inv_dy32)),
+                                          __fmul_rn(__fmul_rn(s, 4.0f), eps))),
+                __fmul_rn(1e-12f, s));
 }
 
 

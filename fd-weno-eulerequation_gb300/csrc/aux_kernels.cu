@@ -73,7 +73,7 @@ __global__ void k_dt_reduce(Geom g, const double *U, Ctrl *c) {
 
 // Pass 1: L = max over nodes of (s32 - e), a lower bound of max s.
 __global__ void k_dt_screen(Geom g, const double *U, Ctrl *c) {
-  if (!c->active) return;
+  if (!c->active || c->bounds_valid) return;
   const long long n = (long long)g.nx * g.ny;
   float lo = 0.0f;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
@@ -95,15 +95,15 @@ __global__ void k_dt_screen(Geom g, const double *U, Ctrl *c) {
 }
 
 // Pass 2: the exact FP64 s of every node with s32 + e >= L (the node holding
-// the maximum is one of them), max-reduced as in k_dt_reduce.
-__global__ void k_dt_refine(Geom g, const double *U, Ctrl *c) {
+// the maximum is one of them), max-reduced as in k_dt_reduce.  With valid
+// per-tile bounds (the last stage of the previous step screened the nodes it
+// wrote) a warp per tile skips the tiles whose upper bound stays below L.
+__global__ void k_dt_refine(Geom g, const double *U, Ctrl *c, const float2 *bounds, int tile_i) {
   if (!c->active) return;
   const float L = __uint_as_float(c->screen_bits);
-  const long long n = (long long)g.nx * g.ny;
   double smax = 0.0;
   int nan_seen = 0;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+  auto visit = [&](int i, int j) {
     const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
     const double rho = U[b], mu = U[g.plane + b], mv = U[2 * g.plane + b], E = U[3 * g.plane + b];
     float s32, e;
@@ -112,6 +112,24 @@ __global__ void k_dt_refine(Geom g, const double *U, Ctrl *c) {
       const double s = dev::exact_speed(g, rho, mu, mv, E);
       if (s != s) nan_seen = 1;
       else if (s > smax) smax = s;
+    }
+  };
+  if (bounds && c->bounds_valid) {
+    const int tiles_j = (g.ny + 31) / 32, ntiles = ((g.nx + tile_i - 1) / tile_i) * tiles_j;
+    const int lane = threadIdx.x & 31;
+    const int warps = int(gridDim.x * blockDim.x) >> 5;
+    for (int t = int(blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += warps) {
+      if (bounds[t].y < L) continue;  // warp-uniform
+      const int i0 = (t / tiles_j) * tile_i, j = (t - (t / tiles_j) * tiles_j) * 32 + lane;
+      const int i1 = i0 + tile_i < g.nx ? i0 + tile_i : g.nx;
+      if (j < g.ny)
+        for (int i = i0; i < i1; ++i) visit(i, j);
+    }
+  } else {
+    const long long n = (long long)g.nx * g.ny;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+      const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+      visit(i, j);
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -141,6 +159,7 @@ __global__ void k_dt_refine(Geom g, const double *U, Ctrl *c) {
 // Open the gate for one host-driven operation (calc_dt, rk_step, step).
 __global__ void k_ctrl_open(Ctrl *c) {
   c->active = 1;
+  c->bounds_valid = 0;
   c->max_s_bits = 0ull;
   c->screen_bits = 0u;
   c->nan_flag = 0;
@@ -180,11 +199,12 @@ __global__ void k_dt_finalize(Ctrl *c) {
 }
 
 // m_now += dt; count++ (src/WENOFD.cpp:238-239), then the loop condition.
-__global__ void k_step_end(Ctrl *c) {
+__global__ void k_step_end(Ctrl *c, int fused) {
   if (!c->active) return;
   c->now += c->dt;
   c->steps += 1;
   c->done = !(fabs(c->now - c->t_end) > 1e-9);
+  c->bounds_valid = fused;
 }
 
 __global__ void k_set_dt(Ctrl *c, double dt) {
@@ -194,6 +214,7 @@ __global__ void k_set_dt(Ctrl *c, double dt) {
 
 __global__ void k_set_time(Ctrl *c, double now) {
   c->now = now;
+  c->bounds_valid = 0;
   c->done = !(fabs(now - c->t_end) > 1e-9);
   c->error = 0;
 }
@@ -204,6 +225,7 @@ __global__ void k_advance_setup(Ctrl *c, long long max_steps) {
   c->max_s_bits = 0ull;
   c->screen_bits = 0u;
   c->nan_flag = 0;
+  c->bounds_valid = 0;
 }
 
 __global__ void k_copy_interior(Geom g, const double *src, double *dst, const int *active) {
@@ -323,10 +345,11 @@ cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream
   return cudaGetLastError();
 }
 
-cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, cudaStream_t s) {
+cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, const float2 *bounds, int tile_i,
+                                      cudaStream_t s) {
   const int grid = grid_for((long long)g.nx * g.ny, 256);
   k_dt_screen<<<grid, 256, 0, s>>>(g, U, c);
-  k_dt_refine<<<grid, 256, 0, s>>>(g, U, c);
+  k_dt_refine<<<grid, 256, 0, s>>>(g, U, c, bounds, tile_i > 0 ? tile_i : 15);
   return cudaGetLastError();
 }
 
@@ -342,8 +365,8 @@ cudaError_t launch_dt_finalize(Ctrl *c, cudaStream_t s) {
   k_dt_finalize<<<1, 1, 0, s>>>(c);
   return cudaGetLastError();
 }
-cudaError_t launch_step_end(Ctrl *c, cudaStream_t s) {
-  k_step_end<<<1, 1, 0, s>>>(c);
+cudaError_t launch_step_end(Ctrl *c, int fused, cudaStream_t s) {
+  k_step_end<<<1, 1, 0, s>>>(c, fused);
   return cudaGetLastError();
 }
 cudaError_t launch_set_dt(Ctrl *c, double dt, cudaStream_t s) {

@@ -103,8 +103,10 @@ int sync(wenofd_solver *s) {
   return WENOFD_OK;
 }
 
+// bounds: this stage writes U^{n+1} at the end of a graph-driven step; its
+// epilogue also screens the next time step (FP32 forms).
 int launch_stage(wenofd_solver *s, const double *in, const double *un, double *out, double a, double b,
-                 double c, int mode) {
+                 double c, int mode, bool bounds = false) {
   StageArgs args;
   args.uin = in;
   args.un = un;
@@ -116,6 +118,10 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   args.active = &s->ctrl->active;
   args.mode = mode;
   args.flags = s->precision == WENOFD_LEARNED ? s->flags : nullptr;
+  if (bounds && s->tile_bounds) {
+    args.bounds = s->tile_bounds;
+    args.screen = &s->ctrl->screen_bits;
+  }
   CUDA_TRY(wenofd::launch_bc_fill(s->g, const_cast<double *>(in), s->special, &s->ctrl->active, s->stream));
   s->launches += 2;
   // The learned form classifies the nodes once per step, on the stage-1
@@ -136,7 +142,8 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
 // RunRK1/2/3 (src/WENOFD.cpp:301-396), dt from the control block.  Stage k
 // reads its input with a halo and writes a different buffer; the last stage
 // writes U^{n+1} over U^n, which it reads only at the node itself.
-int enqueue_rk(wenofd_solver *s) {
+// fused: the last stage also screens the next time step (RK2, RK3).
+int enqueue_rk(wenofd_solver *s, bool fused = false) {
   int rc;
   double *S = s->S, *A = s->A, *B = s->B;
   switch (s->rk) {
@@ -147,11 +154,11 @@ int enqueue_rk(wenofd_solver *s) {
       return WENOFD_OK;
     case 1:
       if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
-      return launch_stage(s, A, S, S, 0.5, 0.5, 0.5, wenofd::kModeRK);
+      return launch_stage(s, A, S, S, 0.5, 0.5, 0.5, wenofd::kModeRK, fused);
     case 2:
       if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
       if ((rc = launch_stage(s, A, S, B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0, wenofd::kModeRK))) return rc;
-      return launch_stage(s, B, S, S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, wenofd::kModeRK);
+      return launch_stage(s, B, S, S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, wenofd::kModeRK, fused);
   }
   return fail(WENOFD_BAD_CONFIG, "Error: Invalid Runge-Kutta method");
 }
@@ -163,7 +170,7 @@ int enqueue_dt_reduce(wenofd_solver *s) {
     CUDA_TRY(wenofd::launch_dt_reduce(s->g, s->S, s->ctrl, s->stream));
     s->launches += 1;
   } else {
-    CUDA_TRY(wenofd::launch_dt_reduce_two_pass(s->g, s->S, s->ctrl, s->stream));
+    CUDA_TRY(wenofd::launch_dt_reduce_two_pass(s->g, s->S, s->ctrl, s->tile_bounds, s->tile_i, s->stream));
     s->launches += 2;
   }
   return WENOFD_OK;
@@ -174,9 +181,10 @@ int enqueue_step(wenofd_solver *s) {
   CUDA_TRY(wenofd::launch_step_begin(s->ctrl, s->stream));
   if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
-  int rc = enqueue_rk(s);
+  const bool fused = s->tile_bounds && s->rk != 0;
+  int rc = enqueue_rk(s, fused);
   if (rc) return rc;
-  CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_step_end(s->ctrl, fused ? 1 : 0, s->stream));
   s->launches += 3;
   return WENOFD_OK;
 }
@@ -221,6 +229,7 @@ void release(wenofd_solver *s) {
   cudaFree(s->flags);
   cudaFree(s->ind_weights);
   cudaFree(s->ind_error);
+  cudaFree(s->tile_bounds);
   cudaFreeHost(s->ctrl_host);
   cudaFreeHost(s->red_host);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -326,6 +335,10 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
             cudaMalloc(&s->ctrl, sizeof(Ctrl)) == cudaSuccess &&
             cudaMallocHost(&s->ctrl_host, sizeof(Ctrl)) == cudaSuccess &&
             cudaMallocHost(&s->red_host, 4 * sizeof(double)) == cudaSuccess;
+  if (ok && precision != WENOFD_FP64) {  // stage tiles of 15 (or 31) x 32 nodes
+    const size_t tiles = size_t((nx + 14) / 15) * size_t((ny + 31) / 32);
+    ok = cudaMalloc(&s->tile_bounds, tiles * sizeof(float2)) == cudaSuccess;
+  }
   if (ok && precision == WENOFD_LEARNED) {
     const size_t fb = size_t(s->g.nxt) * s->g.pitch;
     ok = cudaMalloc(&s->flags, fb) == cudaSuccess &&
@@ -555,7 +568,7 @@ int wenofd_step(wenofd_solver *s, double *dt_out) {
   if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
   if (int rc = enqueue_rk(s)) return rc;
-  CUDA_TRY(wenofd::launch_step_end(s->ctrl, s->stream));
+  CUDA_TRY(wenofd::launch_step_end(s->ctrl, 0, s->stream));
   s->launches += 3;
   if (int rc = read_ctrl(s)) return rc;
   if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");

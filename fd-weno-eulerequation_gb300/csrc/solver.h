@@ -25,6 +25,7 @@ struct wenofd_solver {
   wenofd::Ctrl *ctrl = nullptr;
   wenofd::Ctrl *ctrl_host = nullptr;    // pinned mirror
   double *red_host = nullptr;   // pinned, 4 doubles
+  float2 *tile_bounds = nullptr;  // FP32 forms: per-stage-tile time-step screen bounds
   // learned form (PRECISION 2)
   unsigned char *flags = nullptr;  // [nxt][pitch], ghosts 1
   void *ind_weights = nullptr;     // packed BF16 indicator weights

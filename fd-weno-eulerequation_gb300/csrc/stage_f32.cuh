@@ -14,6 +14,7 @@
 //   Un64 double [4][TI][TJ] the tile's FP64 U^n (stages 2-3, cp.async)
 #pragma once
 
+#include "aux_device.cuh"
 #include "convert.cuh"
 #include "physics.cuh"
 
@@ -165,9 +166,13 @@ __device__ __forceinline__ void cp_async_wait_all_f32() { asm volatile("cp.async
 // node of their stencil line is flagged (a.flags).  COH: inputs may have
 // been written earlier in the same launch by other blocks (persistent
 // batched kernel): loads through L2, U^n read in the epilogue.
+// With a.bounds set (last stage of a step), the epilogue also screens the
+// time step of the nodes it writes (screen_speed) and stores the tile's
+// (max s32 - e, max s32 + e) at a.bounds[tile], raising *a.screen to the
+// tile's lower bound.
 template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false>
 __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a, const int i0, const int j0,
-                                               unsigned char *smem_raw) {
+                                               unsigned char *smem_raw, const int tile = 0) {
   using S = StageSmem32<TI, TJ>;
   constexpr int HI = S::HI, HJ = S::HJ;
   float4 *Us = reinterpret_cast<float4 *>(smem_raw);
@@ -345,6 +350,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     cp_async_wait_all_f32();
     __syncthreads();
   }
+  float lo = 0.0f, hi = 0.0f;  // screen bounds of this thread's nodes
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -360,15 +366,40 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       rr[2] += q.x * 1.0f;
     }
     const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+    double w[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const long long ix = r * g.plane + gidx;
       const double rd = f32_to_f64(rr[r]);
       const double ui = U64[r * TI * TJ + t];
-      if (a.mode == kModeRHS) a.uout[ix] = rd;
-      else if (stage1) a.uout[ix] = fma(cdt, rd, ui);  // a = 1, b = 0: one FMA
-      else if constexpr (COH) a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
-      else a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[r * TI * TJ + t]));
+      if (a.mode == kModeRHS) w[r] = rd;
+      else if (stage1) w[r] = fma(cdt, rd, ui);  // a = 1, b = 0: one FMA
+      else if constexpr (COH) w[r] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
+      else w[r] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[r * TI * TJ + t]));
+      a.uout[ix] = w[r];
+    }
+    if (a.bounds) {
+      float s32, e;
+      screen_speed(g, w[0], w[1], w[2], w[3], s32, e);
+      lo = fmaxf(lo, s32 - e);
+      hi = fmaxf(hi, s32 + e);
+    }
+  }
+  if (a.bounds) {  // block-uniform
+    __shared__ float2 sred[NT / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = fmaxf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = make_float2(lo, hi);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float2 b = sred[0];
+#pragma unroll
+      for (int w = 1; w < NT / 32; ++w) b = make_float2(fmaxf(b.x, sred[w].x), fmaxf(b.y, sred[w].y));
+      a.bounds[tile] = b;
+      atomicMax(a.screen, __float_as_uint(b.x));
     }
   }
 }

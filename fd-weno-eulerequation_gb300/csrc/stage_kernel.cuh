@@ -339,7 +339,8 @@ __global__ void __launch_bounds__(NT, ROUTE && NT <= 256 ? 3 : 1) k_stage(Geom g
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // first interior node of the tile (0-based)
   if constexpr (sizeof(T) == 4)
-    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw,
+                                              int(blockIdx.y * gridDim.x + blockIdx.x));
   else
     stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
 }

@@ -43,6 +43,11 @@ struct Ctrl {
   int done;      // |now - t_end| <= 1e-9 (src/WENOFD.cpp:213)
   int nan_flag;  // a NaN wave speed was seen by the reduction
   int error;     // sticky wenofd_status of the device loop
+  // FP32 forms: the per-tile screen bounds of the current U^n (written by
+  // the last RK stage of the previous step, with their maximum lower bound
+  // in screen_bits) are valid, so the time-step reduction skips its screen
+  // pass.  Cleared at the start of every advance and by every other entry.
+  int bounds_valid;
 };
 
 // Arguments of one RK stage launch.  uin is read with a 3-node halo (its
@@ -60,6 +65,11 @@ struct StageArgs {
   // ghosts 1.  A face takes characteristic WENO-Z when any of the four nodes
   // around it along its line is flagged, else the linear upwind flux.
   const unsigned char *flags = nullptr;
+  // FP32 forms, last stage of a step: per-tile (max s32 - e, max s32 + e)
+  // of the time-step screen over the nodes just written, and the running
+  // maximum lower bound (Ctrl::screen_bits).
+  float2 *bounds = nullptr;
+  unsigned *screen = nullptr;
 };
 enum { kModeRK = 0, kModeRHS = 1 };
 
@@ -134,11 +144,16 @@ cudaError_t launch_dt_reduce(const Geom &g, const double *U, Ctrl *c, cudaStream
 // Same result, bit for bit, in two passes that keep the FP64 pipe nearly
 // idle: an FP32 screen with a rigorous error bound, then FP64 only where a
 // node can hold the maximum.
-cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, cudaStream_t s);
+// With bounds (per-tile screen bounds of stage tiles `tile_i` x 32) and
+// Ctrl::bounds_valid set, the screen pass is skipped and the refine pass
+// visits only the tiles whose upper bound reaches the maximum lower bound.
+cudaError_t launch_dt_reduce_two_pass(const Geom &g, const double *U, Ctrl *c, const float2 *bounds, int tile_i,
+                                      cudaStream_t s);
 cudaError_t launch_ctrl_open(Ctrl *c, cudaStream_t s);
 cudaError_t launch_step_begin(Ctrl *c, cudaStream_t s);
 cudaError_t launch_dt_finalize(Ctrl *c, cudaStream_t s);
-cudaError_t launch_step_end(Ctrl *c, cudaStream_t s);
+// fused: the step's last stage wrote screen bounds of the new U^n
+cudaError_t launch_step_end(Ctrl *c, int fused, cudaStream_t s);
 cudaError_t launch_set_dt(Ctrl *c, double dt, cudaStream_t s);
 cudaError_t launch_set_time(Ctrl *c, double now, cudaStream_t s);
 cudaError_t launch_advance_setup(Ctrl *c, long long max_steps, cudaStream_t s);

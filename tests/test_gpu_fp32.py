@@ -88,3 +88,39 @@ def test_two_pass_time_step_equals_fp64_reduction(tc, n, steps):
             s.set_state(U)
             dts.append(s.calc_dt())
     assert dts[0] == dts[1] == dts[2] == p.calc_dt()
+
+
+@pytest.mark.parametrize("precision", [wenofd.FP32, wenofd.LEARNED])
+@pytest.mark.parametrize("tile_i", [0, 31])
+def test_fused_screen_steps_equal_separate_steps(precision, tile_i):
+    """Inside wenofd_advance the last RK stage of a step also screens the
+    next time step per stage tile, and the reduction then refines only the
+    tiles that can hold the maximum.  The steps must equal, bit for bit,
+    steps driven one call at a time (calc_dt: full screen + refine; rk_step)."""
+    import mlp_oracle
+
+    n, steps = 200, 8
+    cfg = {"TESTCASE": 5, "ELEMNUMX": n, "ELEMNUMY": n + 17, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1, "SEED": 5,
+           "PRECISION": precision, "TILE_I": tile_i}
+    params = mlp_oracle.init_params(3)
+
+    def make():
+        s = wenofd.Solver(cfg)
+        s.initialize()
+        if precision == wenofd.LEARNED:
+            s.set_indicator(params, 0.5)
+        return s
+
+    with make() as a:
+        assert a.advance(max_steps=steps) == steps
+        Ua, ta = a.get_state(), a.info().now
+    with make() as b:
+        now = 0.0
+        for _ in range(steps):
+            dt = b.calc_dt()
+            b.rk_step(dt)
+            now += dt
+            b.set_time(now)
+        Ub = b.get_state()
+    assert ta == now
+    assert np.array_equal(Ua, Ub)
