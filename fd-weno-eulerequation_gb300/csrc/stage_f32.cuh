@@ -21,13 +21,17 @@
 namespace wenofd {
 namespace dev {
 
-template <int TI, int TJ>
+// KEEP: the tile's FP64 input values and U^n are staged in shared memory
+// (U64, Un64); without KEEP the epilogue reads them from global memory
+// (cached, just loaded with the halo), which frees 2 x 15 KB per block for
+// a fourth resident block.
+template <int TI, int TJ, bool KEEP = true>
 struct StageSmem32 {
   static constexpr int HI = TI + 6, HJ = TJ + 6;
   static constexpr int kU = HI * HJ;
   static constexpr int kSplit = HI * TJ > TI * HJ ? HI * TJ : TI * HJ;
   static constexpr int kFace = (TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1);
-  static constexpr int kKeep = 2 * 4 * TI * TJ;  // doubles
+  static constexpr int kKeep = KEEP ? 2 * 4 * TI * TJ : 0;  // doubles
   static constexpr size_t bytes = sizeof(float4) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
 };
 
@@ -170,10 +174,10 @@ __device__ __forceinline__ void cp_async_wait_all_f32() { asm volatile("cp.async
 // time step of the nodes it writes (screen_speed) and stores the tile's
 // (max s32 - e, max s32 + e) at a.bounds[tile], raising *a.screen to the
 // tile's lower bound.
-template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false>
+template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false, bool KEEP = true>
 __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a, const int i0, const int j0,
                                                unsigned char *smem_raw, const int tile = 0) {
-  using S = StageSmem32<TI, TJ>;
+  using S = StageSmem32<TI, TJ, KEEP>;
   constexpr int HI = S::HI, HJ = S::HJ;
   float4 *Us = reinterpret_cast<float4 *>(smem_raw);
   float4 *Fp = Us + S::kU;
@@ -191,7 +195,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
 
   // stages 2 and 3: fetch this tile's U^n now, used only by the epilogue
-  if constexpr (!COH) {
+  if constexpr (!COH && KEEP) {
     if (a.mode == kModeRK && !stage1) {
       for (int t = threadIdx.x; t < 4 * TI * TJ; t += NT) {
         const int r = t / (TI * TJ), q = t - r * (TI * TJ);
@@ -240,10 +244,12 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       if (t < HI * HJ) {
         Us[t] = make_float4(f64_to_f32(v[k][0]), f64_to_f32(v[k][1]), f64_to_f32(v[k][2]), f64_to_f32(v[k][3]));
         const int hi = t / HJ, hj = t - (t / HJ) * HJ;
-        if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
-          const int q = (hi - 3) * TJ + hj - 3;
+        if constexpr (KEEP) {
+          if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
+            const int q = (hi - 3) * TJ + hj - 3;
 #pragma unroll
-          for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = v[k][r];
+            for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = v[k][r];
+          }
         }
       }
     }
@@ -346,7 +352,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   // --- y term, source, RK combination in FP64, store
   const double dt = COH ? __ldcg(a.dt) : *a.dt;
   const double cdt = a.c * dt;
-  if constexpr (!COH) {
+  if constexpr (!COH && KEEP) {
     cp_async_wait_all_f32();
     __syncthreads();
   }
@@ -366,16 +372,30 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       rr[2] += q.x * 1.0f;
     }
     const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+    double ui[4], un[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const long long ix = r * g.plane + gidx;
+      if constexpr (KEEP) {
+        ui[r] = U64[r * TI * TJ + t];
+        if constexpr (COH) un[r] = __ldcg(&a.un[ix]);
+        else un[r] = Un64[r * TI * TJ + t];
+      } else if constexpr (COH) {
+        ui[r] = __ldcg(&a.uin[ix]);
+        un[r] = __ldcg(&a.un[ix]);
+      } else {
+        ui[r] = __ldg(&a.uin[ix]);
+        if (!stage1) un[r] = __ldg(&a.un[ix]);
+      }
+    }
     double w[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const long long ix = r * g.plane + gidx;
       const double rd = f32_to_f64(rr[r]);
-      const double ui = U64[r * TI * TJ + t];
       if (a.mode == kModeRHS) w[r] = rd;
-      else if (stage1) w[r] = fma(cdt, rd, ui);  // a = 1, b = 0: one FMA
-      else if constexpr (COH) w[r] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
-      else w[r] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[r * TI * TJ + t]));
+      else if (stage1) w[r] = fma(cdt, rd, ui[r]);  // a = 1, b = 0: one FMA
+      else w[r] = fma(cdt, rd, fma(a.b, ui[r], a.a * un[r]));
       a.uout[ix] = w[r];
     }
     if (a.bounds) {
