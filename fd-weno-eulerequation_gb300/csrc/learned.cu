@@ -145,16 +145,20 @@ __global__ void k_adam(float *P, const float *G, float *M, float *V, int step, f
 // One CTA of 128 threads runs tiles of 4 x 32 cells (x by y).  Per tile:
 //   1. density and pressure of the 8 x 36 node patch around the tile -> smem;
 //   2. each thread builds its cell's 50 features and writes them as BF16
-//      into A1 [128 x 64]: columns 50 and 51 hold 1.0 so that the bias of
-//      layer 1 (split into a BF16 high and low part, columns 50 and 51 of
-//      W1) is added by the tensor core; the rest is zero padding.  Operands
-//      use the no-swizzle K-major layout: 8-row x 16-byte core matrices,
-//      K-adjacent cores 128 B apart (LBO), 8-row groups KC*128 B apart (SBO);
+//      into A1 [128 x 64]: the 25 density features in columns 0..24, 1.0 in
+//      columns 25 and 26 so that the bias of layer 1 (split into a BF16
+//      high and low part, the same columns of W1) is added by the tensor
+//      core, the 25 pressure features in columns 32..56, zeros elsewhere;
+//      each window's features go out in 16-byte chunks as they are formed.
+//      Operands use the no-swizzle K-major layout: 8-row x 16-byte core
+//      matrices, K-adjacent cores 128 B apart (LBO), 8-row groups KC*128 B
+//      apart (SBO);
 //   3. one thread issues 4 x tcgen05.mma (M=128, N=32, K=16, BF16 in, FP32
 //      accumulate): D1 = A1 * W1^T into tensor-memory columns [0, 32);
 //   4. each warp reads its 32 rows back (tcgen05.ld 32x32b.x32), applies
 //      GELU in packed BF16 pairs and writes A2 [128 x 48] (columns 32 and 33
-//      are 1.0 for the bias of layer 2, the rest zero);
+//      are 1.0 for the bias of layer 2, the rest zero) over A1, which layer 1
+//      has finished reading;
 //   5. 3 x tcgen05.mma: D2 = A2 * W2^T into columns [32, 64);
 //   6. read back, GELU, write the activations over A2;
 //   7. 3 x tcgen05.mma (N = 16): D3 = A2 * W3^T into columns [0, 16), with
@@ -163,14 +167,21 @@ __global__ void k_adam(float *P, const float *G, float *M, float *V, int step, f
 // MMA completion is signalled through an mbarrier (tcgen05.commit); every
 // wait on it is bounded and on give-up the kernel records an error and
 // stops issuing work, then releases its tensor memory.
+//
+// Occupancy: 27 KB of shared memory, at most 64 registers and 64 tensor-
+// memory columns per CTA, so eight CTAs (32 warps) share an SM and its 512
+// tensor-memory columns; their load, CUDA-core and tensor-core phases
+// overlap.
 
 constexpr int kTileI = 4, kTileJ = 32, kCells = kTileI * kTileJ;  // 128 = MMA M
 constexpr int kPI = kTileI + 4, kPJ = kTileJ + 4;                   // node patch
 constexpr int kK1 = 64, kK2 = 48, kN3 = 16;
 constexpr unsigned kWaitLimit = 1u << 22;
 
+constexpr int kColBias1 = 25, kColP = 32;  // A1 / W1 columns: bias 1 (hi, lo), first pressure feature
+
 struct IndicatorWeights {  // device buffer prepared by the host (BF16, canonical layout)
-  __nv_bfloat16 w1[kHid * kK1];  // [32 x 64]: W1 | b1 hi | b1 lo | 0
+  __nv_bfloat16 w1[kHid * kK1];  // [32 x 64]: W1 rho part | b1 hi | b1 lo | 0 | W1 p part | 0
   __nv_bfloat16 w2[kHid * kK2];  // [32 x 48]: W2 | b2 hi | b2 lo | 0
   __nv_bfloat16 w3[kN3 * kK2];   // [16 x 48]: row 0 w3 hi | b3 hi | b3 lo, row 1 w3 lo, rest 0
 };
@@ -281,9 +292,10 @@ __device__ __forceinline__ unsigned gelu_bf16x2(float z0, float z1) {
   return bf2_bits(__hfma2(h, bits_bf2(t), h));
 }
 
-// GELU of the 32 accumulator columns of this thread's row into 4 x 16-byte
-// chunks (columns 0..31) of a canonical-layout operand with KC core columns.
-__device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row, int kc) {
+// GELU of the 32 accumulator columns of this thread's row into columns
+// 0..31 of A2 [128 x 48], and columns 32..47 = 1, 1, 0, ... (bias inputs).
+__device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row) {
+  constexpr int kc = kK2 / 8;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     uint4 q;
@@ -293,14 +305,44 @@ __device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 
     q.w = gelu_bf16x2(z[8 * c + 6], z[8 * c + 7]);
     *reinterpret_cast<uint4 *>(&A[canon_off(row, 8 * c, kc)]) = q;
   }
+  *reinterpret_cast<uint4 *>(&A[canon_off(row, 32, kc)]) = make_uint4(0x3F803F80u, 0u, 0u, 0u);  // two BF16 1.0
+  *reinterpret_cast<uint4 *>(&A[canon_off(row, 40, kc)]) = make_uint4(0u, 0u, 0u, 0u);
 }
 
-__global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
-                                                         float logit_threshold, unsigned char *flags, int flag_pitch,
-                                                         int *error, const int *active) {
+// Normalised 5x5 window (normalise() in learned_common.cuh, same arithmetic)
+// written as BF16 into columns col0 .. col0+24 of row `row` of A1 in four
+// 16-byte chunks; columns col0+25 .. col0+31 take `tail` (two values, then
+// zeros).
+__device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A, int row, int col0, float tail0,
+                                             float tail1) {
+  constexpr int kc = kK1 / 8;
+  const float c = w[12];
+  float R = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 25; ++k) R = fmaxf(R, fabsf(w[k] - c));
+  const bool flat = R <= kFlat * (fabsf(c) + 1e-12f);
+  const float inv = flat ? 0.0f : 1.0f / R;
+  auto val = [&](int k) -> float {
+    if (k < 25) return flat ? 0.0f : (w[k] - c) * inv;
+    return k == 25 ? tail0 : (k == 26 ? tail1 : 0.0f);
+  };
+#pragma unroll
+  for (int ch = 0; ch < 4; ++ch) {
+    uint4 q;
+    q.x = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 0), val(8 * ch + 1)));
+    q.y = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 2), val(8 * ch + 3)));
+    q.z = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 4), val(8 * ch + 5)));
+    q.w = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 6), val(8 * ch + 7)));
+    *reinterpret_cast<uint4 *>(&A[canon_off(row, col0 + 8 * ch, kc)]) = q;
+  }
+}
+
+__global__ void __launch_bounds__(kCells, 8) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
+                                                            float logit_threshold, unsigned char *flags,
+                                                            int flag_pitch, int *error, const int *active) {
   if (active && *active == 0) return;
-  __shared__ __align__(128) __nv_bfloat16 sA1[kCells * kK1];
-  __shared__ __align__(128) __nv_bfloat16 sA2[kCells * kK2];
+  __shared__ __align__(128) __nv_bfloat16 sA[kCells * kK1];  // A1, then A2 [128 x 48] (and the layer-3 input)
+  __nv_bfloat16 *const sA1 = sA, *const sA2 = sA;
   __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
   __shared__ __align__(128) __nv_bfloat16 sB2[kHid * kK2];
   __shared__ __align__(128) __nv_bfloat16 sB3[kN3 * kK2];
@@ -312,11 +354,6 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
   for (int k = tid; k < kHid * kK1; k += kCells) sB1[k] = W->w1[k];
   for (int k = tid; k < kHid * kK2; k += kCells) sB2[k] = W->w2[k];
   for (int k = tid; k < kN3 * kK2; k += kCells) sB3[k] = W->w3[k];
-  {  // constant columns 32..47 of this thread's row of A2: 1, 1, 0, ...
-    const unsigned one2 = 0x3F803F80u;  // two BF16 1.0
-    *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 32, kK2 / 8)]) = make_uint4(one2, 0u, 0u, 0u);
-    *reinterpret_cast<uint4 *>(&sA2[canon_off(tid, 40, kK2 / 8)]) = make_uint4(0u, 0u, 0u, 0u);
-  }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -393,34 +430,20 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
       }
     }
     __syncthreads();
-    // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1; columns 50, 51 = 1
+    // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1
     {
       const int ci = warp, cj = tid & 31;
-      float f[kK1];
       float w[25];
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
         for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[(ci + a) * kPJ + cj + b];
-      normalise(w, f);
+      window_store(w, sA1, tid, 0, 1.0f, 1.0f);  // columns 25, 26: bias inputs
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
         for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[(ci + a) * kPJ + cj + b];
-      normalise(w, f + 25);
-      f[50] = 1.0f;
-      f[51] = 1.0f;
-#pragma unroll
-      for (int k = 52; k < kK1; ++k) f[k] = 0.0f;
-#pragma unroll
-      for (int c = 0; c < kK1 / 8; ++c) {
-        uint4 q;
-        q.x = bf2_bits(__floats2bfloat162_rn(f[8 * c + 0], f[8 * c + 1]));
-        q.y = bf2_bits(__floats2bfloat162_rn(f[8 * c + 2], f[8 * c + 3]));
-        q.z = bf2_bits(__floats2bfloat162_rn(f[8 * c + 4], f[8 * c + 5]));
-        q.w = bf2_bits(__floats2bfloat162_rn(f[8 * c + 6], f[8 * c + 7]));
-        *reinterpret_cast<uint4 *>(&sA1[canon_off(tid, 8 * c, kK1 / 8)]) = q;
-      }
+      window_store(w, sA1, tid, kColP, 0.0f, 0.0f);
     }
     // 3. layer 1 (bias included)
     if (!layer([&] { mma_layer<kK1, kHid>(tmem, sA1, sB1); })) break;
@@ -428,7 +451,7 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
     {
       float z[32];
       tmem_ld32(tmem + lane_base, z);
-      gelu_row_store(z, sA2, tid, kK2 / 8);
+      gelu_row_store(z, sA2, tid);
     }
     // 5. layer 2
     if (!layer([&] { mma_layer<kK2, kHid>(tmem + 32, sA2, sB2); })) break;
@@ -436,7 +459,7 @@ __global__ void __launch_bounds__(kCells) k_indicator_tc(Geom g, const double *U
     {
       float z[32];
       tmem_ld32(tmem + lane_base + 32, z);
-      gelu_row_store(z, sA2, tid, kK2 / 8);
+      gelu_row_store(z, sA2, tid);
     }
     // 7. output layer on the tensor cores, into the columns of D1
     if (!layer([&] { mma_layer<kK2, kN3>(tmem, sA2, sB3); })) break;
@@ -487,10 +510,11 @@ void pack_indicator_weights(const float *params, void *host_out) {
   };
   float hi, lo;
   for (int o = 0; o < kHid; ++o) {
-    for (int k = 0; k < kIn; ++k) put(w->w1, o, k, kK1 / 8, params[oW1 + o * kIn + k]);
+    for (int k = 0; k < kIn; ++k)  // density features 0..24 -> columns 0..24, pressure 25..49 -> 32..56
+      put(w->w1, o, k < 25 ? k : kColP + (k - 25), kK1 / 8, params[oW1 + o * kIn + k]);
     hi_lo(params[oB1 + o], hi, lo);
-    put(w->w1, o, kIn, kK1 / 8, hi);
-    put(w->w1, o, kIn + 1, kK1 / 8, lo);
+    put(w->w1, o, kColBias1, kK1 / 8, hi);
+    put(w->w1, o, kColBias1 + 1, kK1 / 8, lo);
     for (int k = 0; k < kHid; ++k) put(w->w2, o, k, kK2 / 8, params[oW2 + o * kHid + k]);
     hi_lo(params[oB2 + o], hi, lo);
     put(w->w2, o, kHid, kK2 / 8, hi);
