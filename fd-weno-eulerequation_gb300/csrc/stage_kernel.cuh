@@ -334,12 +334,12 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
 // characteristic-WENO path runs for a few percent of the faces, so trading
 // registers on that path for occupancy everywhere else pays.
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT, ROUTE && NT <= 256 ? 4 : 1) k_stage(Geom g, StageArgs a) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 && NT <= 256 ? (ROUTE ? 4 : 3) : 1) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // first interior node of the tile (0-based)
   if constexpr (sizeof(T) == 4)
-    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, !(ROUTE && NT <= 256)>(
+    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, !(NT <= 256)>(
         g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x));
   else
     stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(NT, ROUTE && NT <= 256 ? 4 : 1) k_stage(Geom g
 // Dynamic shared memory of one stage tile.
 template <typename T, int TI, int TJ, bool ROUTE = false, int NT = 256>
 constexpr size_t stage_smem_bytes() {
-  if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ, !(ROUTE && NT <= 256)>::bytes;
+  if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ, !(NT <= 256)>::bytes;
   else return StageSmem<T, TI, TJ>::bytes;
 }
 
