@@ -253,6 +253,9 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   if (!get_int(opt, "DEVICE", device, false)) return fail(WENOFD_BAD_CONFIG, "bad DEVICE");
   if (!get_int(opt, "TILE_I", tile_i, false)) return fail(WENOFD_BAD_CONFIG, "bad TILE_I");
   if (!get_double(opt, "TEND", t_end, false)) return fail(WENOFD_BAD_CONFIG, "bad TEND");
+  double label_deviation = 1e-2;
+  if (!get_double(opt, "LABEL_DEVIATION", label_deviation, false) || !(label_deviation > 0.0))
+    return fail(WENOFD_BAD_CONFIG, "bad LABEL_DEVIATION");
   {
     auto it = opt.find("SEED");
     if (it != opt.end()) {
@@ -308,6 +311,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   s->precision = precision;
   s->tile_i = tile_i;
   s->cfl = cfl;
+  s->label_deviation = label_deviation;
   s->cs = cs;
   const double dx = (cs.xr - cs.xl) / (nx - 1);  // src/WENOFD.cpp:73-74
   const double dy = (cs.yr - cs.yl) / (ny - 1);
@@ -725,7 +729,7 @@ int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
   if (dev_features) CUDA_TRY(wenofd::launch_features(s->g, s->S, dev_features, s->stream));
-  if (dev_labels) CUDA_TRY(wenofd::launch_labels(s->g, s->S, dev_labels, s->stream));
+  if (dev_labels) CUDA_TRY(wenofd::launch_labels(s->g, s->S, dev_labels, s->label_deviation, s->stream));
   return sync(s);
 }
 

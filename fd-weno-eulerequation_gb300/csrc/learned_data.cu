@@ -102,7 +102,7 @@ __device__ double face_deviation(const Geom &g, const double *U, int ei, int ej)
   return dev;
 }
 
-__global__ void k_labels(Geom g, const double *U, unsigned char *labels) {
+__global__ void k_labels(Geom g, const double *U, unsigned char *labels, double deviation) {
   const long long n = (long long)g.nx * g.ny;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
     const int ei = kGhost + int(c / g.ny), ej = kGhost + int(c - (c / g.ny) * g.ny);
@@ -110,7 +110,7 @@ __global__ void k_labels(Geom g, const double *U, unsigned char *labels) {
     d = fmax(d, face_deviation<0>(g, U, ei + 1, ej));
     d = fmax(d, face_deviation<1>(g, U, ei, ej));
     d = fmax(d, face_deviation<1>(g, U, ei, ej + 1));
-    labels[c] = d > 1e-2 ? 1 : 0;
+    labels[c] = d > deviation ? 1 : 0;
   }
 }
 
@@ -122,8 +122,8 @@ cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStr
   return cudaGetLastError();
 }
 
-cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, cudaStream_t s) {
-  lrn::k_labels<<<lrn::grid_for((long long)g.nx * g.ny, 128, 152 * 32), 128, 0, s>>>(g, U, labels);
+cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, double deviation, cudaStream_t s) {
+  lrn::k_labels<<<lrn::grid_for((long long)g.nx * g.ny, 128, 152 * 32), 128, 0, s>>>(g, U, labels, deviation);
   return cudaGetLastError();
 }
 

@@ -31,6 +31,7 @@ struct wenofd_solver {
   void *ind_weights = nullptr;     // packed BF16 indicator weights
   int *ind_error = nullptr;
   float ind_logit_threshold = 0.0f;
+  double label_deviation = 1e-2;  // LABEL_DEVIATION: training-label threshold
   bool ind_ready = false;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;

@@ -134,7 +134,8 @@ cudaError_t launch_batch_gather(const BatchMember *members, int n, BatchMemberSt
 size_t indicator_weights_bytes();
 void pack_indicator_weights(const float *params, void *host_out);
 cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStream_t s);
-cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, cudaStream_t s);
+// labels: 1 where a face of the node has a WENO-Z weight deviation above `deviation`
+cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, double deviation, cudaStream_t s);
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
                              unsigned char *flags, int *error, const int *active, cudaStream_t s);
 

@@ -27,7 +27,8 @@ DEFAULT_RUNS = ((5, 11), (5, 12), (4, 13), (4, 14))
 
 
 def generate_dataset(torch, runs=DEFAULT_RUNS, n: int = 512, snapshots=(40, 120, 240, 400),
-                     per_snapshot: int = 125_000, device: int = 0, sample_seed: int = 0):
+                     per_snapshot: int = 125_000, device: int = 0, sample_seed: int = 0,
+                     label_deviation: float = 1e-2):
     """Features X (N, 50) and labels y (N,) as CUDA float32 tensors: for each
     (testcase, seed) run, an FP32-form solve at n x n, and at each snapshot
     step a sample of `per_snapshot` cells, half flagged and half not where
@@ -41,7 +42,8 @@ def generate_dataset(torch, runs=DEFAULT_RUNS, n: int = 512, snapshots=(40, 120,
     lab = torch.empty(cells, dtype=torch.uint8, device=f"cuda:{device}")
     for testcase, seed in runs:
         with Solver({"TESTCASE": testcase, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
-                     "SEED": seed, "PRECISION": FP32, "DEVICE": device, "TEND": 1.0e9}) as s:
+                     "SEED": seed, "PRECISION": FP32, "DEVICE": device, "TEND": 1.0e9,
+                     "LABEL_DEVIATION": label_deviation}) as s:
             s.initialize()
             done = 0
             for snap in snapshots:

@@ -73,9 +73,11 @@ const char *wenofd_version(void);
 /* CConfig::read + CWENOFD::initializeSolver (utils/readConfig.hpp:39-80,
  * src/WENOFD.cpp:10-164).  keys/values are the config.cfg pairs; required:
  * TESTCASE, ELEMNUMX, ELEMNUMY, RKMETH, CFL, SCHEME (src/WENOFD.cpp:24-40).
- * Optional keys the reference does not have: PRECISION (0 FP64, 1 FP32),
- * SEED (seeded cases), TEND (overrides equation->outputtime), DEVICE,
- * TILE_I (stage-kernel tile height; 0 = default), and overrides of the
+ * Optional keys the reference does not have: PRECISION (0 FP64, 1 FP32,
+ * 2 learned + FP32), SEED (seeded cases), TEND (overrides
+ * equation->outputtime), DEVICE, TILE_I (stage-kernel tile height; 0 =
+ * default), LABEL_DEVIATION (training labels of wenofd_indicator_data;
+ * default 1e-2), and overrides of the
  * EulerEquation members the reference's callers may set on their equation
  * object (utils/equations.hpp:58-70): XL, XR, YL, YR, GAMMA, BC_LEFT,
  * BC_RIGHT, BC_BOTTOM, BC_TOP (BOUNDARYTYPE values), GRAVITY (0/1). */
@@ -163,8 +165,8 @@ int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float thres
 int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags);
 /* Training data of the current state: features [NX*NY][50] float and labels
  * [NX*NY] bytes (1 where WENO-Z's nonlinear weights differ from the linear
- * ones by more than 1e-2 on a non-flat stencil at any of the node's four
- * faces), device pointers; either may be NULL. */
+ * ones by more than LABEL_DEVIATION, default 1e-2, on a non-flat stencil at
+ * any of the node's four faces), device pointers; either may be NULL. */
 int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *dev_labels);
 /* FP32 training kernels on device buffers (stream-ordered):
  *   forward: logits[n] of samples x[n][50];

@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
         L.orc_conservation_sums.argtypes = [C.POINTER(Grid), P, P]
         L.orc_cell_features.argtypes = [C.POINTER(Grid), P, C.POINTER(C.c_float)]
         L.orc_cell_labels.argtypes = [C.POINTER(Grid), P, C.POINTER(C.c_ubyte)]
+        L.orc_cell_labels_at.argtypes = [C.POINTER(Grid), P, C.POINTER(C.c_ubyte), D]
         _lib = L
     return _lib
 
@@ -202,11 +203,13 @@ class Problem:
         lib().orc_cell_features(C.byref(self.grid), _p(self.U), out.ctypes.data_as(C.POINTER(C.c_float)))
         return out
 
-    def cell_labels(self) -> np.ndarray:
-        """(NX*NY,) uint8 WENO-Z weight-deviation labels of the current state."""
+    def cell_labels(self, deviation: float = 1e-2) -> np.ndarray:
+        """(NX*NY,) uint8 WENO-Z weight-deviation labels of the current state
+        (1 where a face of the node deviates by more than `deviation`)."""
         self.fill_boundary()
         out = np.zeros(self.nx * self.ny, dtype=np.uint8)
-        lib().orc_cell_labels(C.byref(self.grid), _p(self.U), out.ctypes.data_as(C.POINTER(C.c_ubyte)))
+        lib().orc_cell_labels_at(C.byref(self.grid), _p(self.U), out.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                                 deviation)
         return out
 
     def conservation_sums(self) -> np.ndarray:

@@ -879,6 +879,12 @@ static double face_deviation(const orc_grid *g, const double *U, int dir, int ei
 }
 
 void orc_cell_labels(const orc_grid *g, const double *U, unsigned char *labels) {
+  orc_cell_labels_at(g, U, labels, 1e-2);
+}
+
+/* The same with the deviation above which a node is labelled as a
+ * parameter. */
+void orc_cell_labels_at(const orc_grid *g, const double *U, unsigned char *labels, double deviation) {
   for (int i = 0; i < g->nx; ++i)
     for (int j = 0; j < g->ny; ++j) {
       const int ei = ORC_NG + i, ej = ORC_NG + j;
@@ -889,6 +895,6 @@ void orc_cell_labels(const orc_grid *g, const double *U, unsigned char *labels) 
       if (d2 > dev) dev = d2;
       d2 = face_deviation(g, U, 1, ei, ej + 1);
       if (d2 > dev) dev = d2;
-      labels[(size_t)i * g->ny + j] = dev > 1e-2;
+      labels[(size_t)i * g->ny + j] = dev > deviation;
     }
 }

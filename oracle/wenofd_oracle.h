@@ -104,6 +104,7 @@ void orc_conservation_sums(const orc_grid *g, const double *U, double out[4]);
  *    of the largest characteristic magnitude at the face.  FP64. */
 void orc_cell_features(const orc_grid *g, const double *U, float *features);
 void orc_cell_labels(const orc_grid *g, const double *U, unsigned char *labels);
+void orc_cell_labels_at(const orc_grid *g, const double *U, unsigned char *labels, double deviation);
 
 unsigned long long orc_splitmix64(unsigned long long *state);
 double orc_uniform01(unsigned long long *state);
