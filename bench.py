@@ -242,6 +242,11 @@ def finer_reference_errors(wenofd, params, device: int, n: int = 513, t_end: flo
     e["riemann"] = r
     return e
 
+# Uneven members of the batching leg: seeded four-quadrant Riemann problems.
+BATCH_SHAPES = [(128, 128), (256, 256), (512, 512), (1024, 1024), (192, 320), (384, 256), (96, 640), (768, 512)]
+BATCH_MEMBERS = 64
+
+
 def batching_leg(wenofd, precision: int, device: int, steps: int, warmup: int) -> dict:
     """Aggregate cell-updates/s of BATCH_MEMBERS independent solves of uneven
     sizes: one persistent kernel per launch (wenofd_batch_advance, autotuned)

@@ -142,7 +142,7 @@ __device__ __forceinline__ int runnable(const Ctrl *c) {
 }
 
 template <typename T, int SCHEME, int TI, int NT>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 512 / NT : 1) k_batch(BatchArgs b) {
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) k_batch(BatchArgs b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BatchMember sM;
   constexpr int TJ = 32;
@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 512 / NT : 1) k_batch(Bat
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
         a.flags = nullptr;
-        if constexpr (F32) stage_tile_f32<SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
+        if constexpr (F32)
+          stage_tile_f32<SCHEME, TI, TJ, NT, false, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
         else stage_tile<T, SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < 2) {
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 512 / NT : 1) k_batch(Bat
 // from that query.
 template <typename T, int TI, int NT>
 cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm, cudaStream_t s, int *grid) {
-  constexpr size_t smem = stage_smem_bytes<T, TI, 32>();
+  constexpr size_t smem = stage_smem_bytes<T, TI, 32, false, NT>();
   void (*fn)(BatchArgs) = nullptr;
   switch (scheme) {
     case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT>; break;
