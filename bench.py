@@ -322,6 +322,8 @@ def main() -> None:
                     help="WENO-Z weight deviation that labels a training node")
     ap.add_argument("--only-batching", action="store_true",
                     help="run the batching leg only (FP32 and FP64 batches vs one at a time): for profiling")
+    ap.add_argument("--only-fp32", action="store_true",
+                    help="time the FP32 form only (no training, no other legs): for profiling")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (no other legs, errors, e2e or CPU leg): for profiling")
     args = ap.parse_args()
@@ -361,6 +363,14 @@ def main() -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.only_fp32:
+        s32, ms32, launches = time_form(wenofd, torch, wenofd.FP32, local, args.steps, args.warmup, stream)
+        s32.close()
+        if rank == 0:
+            print(json.dumps({"fp32_form": {"value": args.steps * cells / (ms32 / 1e3), "unit": "cell-updates/s",
+                                            "ms_per_step": ms32 / args.steps, "gpu_launches": launches},
+                              "note": "FP32 form only (profiling run)"}))
+        return
     if args.only_batching:
         out = {"fp32": batching_leg(wenofd, wenofd.FP32, local, args.steps, args.warmup),
                "fp64": batching_leg(wenofd, wenofd.FP64, local, 2, args.warmup)}
