@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         a.flags = nullptr;
         if constexpr (F32)
           stage_tile_f32<SCHEME, TI, TJ, NT, false, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
-        else stage_tile<T, SCHEME, TI, TJ, NT, false, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
+        else stage_tile_f64<SCHEME, TI, TJ, NT, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < 2) {
         grid_barrier(b, Nothing());

@@ -19,8 +19,9 @@ __device__ __forceinline__ float tsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double tabs(double x) { return fabs(x); }
 __device__ __forceinline__ float tabs(float x) { return fabsf(x); }
 
-// Division.  FP64: IEEE '/'.  FP32 form: full-precision reciprocal-based
-// division (the FP32 form is not bitwise and does not need IEEE rounding).
+// Division.  FP64: IEEE '/'.  FP32 form: __fdividef, reciprocal times
+// numerator (about 2 ulp; the FP32 form is not bitwise and does not need
+// IEEE rounding).
 __device__ __forceinline__ double tdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float tdiv(float a, float b) { return __fdividef(a, b); }
 

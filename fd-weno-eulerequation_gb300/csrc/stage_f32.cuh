@@ -1,5 +1,5 @@
 // One RK stage tile of the FP32 precision form (and of the learned form,
-// ROUTE), the FP32 counterpart of stage_tile in stage_kernel.cuh with the
+// ROUTE), the FP32 counterpart of stage_tile_f64 in stage_kernel.cuh with the
 // same phases and the same per-face arithmetic, laid out for the FP32 pipe:
 // every node's four conserved components (and its split fluxes, and every
 // face's flux) sit together as one float4 in shared memory, so a stencil
@@ -47,9 +47,10 @@ __device__ __forceinline__ void split4(float gamma, const float4 q, float4 &fm, 
   fp = make_float4(p[0], p[1], p[2], p[3]);
 }
 
-// Linear fifth-order upwind flux of all four components (linear_upwind in
-// stage_kernel.cuh, same coefficients and order): P0..P4 = F+ at nodes
-// face-3..face+1, M0..M4 = F- at nodes face-2..face+2.
+// Linear fifth-order upwind flux of one component: WENO with its weights
+// frozen at (0.1, 0.6, 0.3), on F+ at nodes face-3..face+1 (p0..p4) and on F-
+// mirrored (nodes face+2..face-2, m4..m0): (2a - 13b + 47c + 27d - 3e) / 60
+// each.
 __device__ __forceinline__ float lin5(float p0, float p1, float p2, float p3, float p4, float m0, float m1, float m2,
                                       float m3, float m4) {
   const float c0 = float(2.0 / 60.0), c1 = float(-13.0 / 60.0), c2 = float(47.0 / 60.0), c3 = float(27.0 / 60.0),

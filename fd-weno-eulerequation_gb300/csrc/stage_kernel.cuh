@@ -15,6 +15,10 @@
 // y-faces, and keeps the per-node x term in registers between the sweeps.
 // Shared-memory regions for the split fluxes and face fluxes are reused by
 // the y sweep.
+//
+// This file holds the FP64 tile (bitwise the reference) and the kernel and
+// launcher shared by both precisions; the FP32 tile (FP32 form and learned
+// form) is stage_f32.cuh.
 #pragma once
 
 #include "convert.cuh"
@@ -24,79 +28,35 @@
 namespace wenofd {
 namespace dev {
 
-template <typename T, int TI, int TJ>
+// Shared memory of the FP64 tile, structure of arrays [component][row][col].
+template <int TI, int TJ>
 struct StageSmem {
   static constexpr int HI = TI + 6, HJ = TJ + 6;
   static constexpr int kU = 4 * HI * HJ;                                    // state + halo
   static constexpr int kSplit = 4 * (HI * TJ > TI * HJ ? HI * TJ : TI * HJ);  // one of F+, F-
   static constexpr int kFace = 4 * ((TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1));
-  // FP32 form: the tile's FP64 input values (kept from the halo load) and
-  // its FP64 U^n values (prefetched with cp.async) for the RK combination.
-  static constexpr int kKeep = sizeof(T) == 4 ? 2 * 4 * TI * TJ : 0;
-  static constexpr size_t bytes = sizeof(T) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
+  static constexpr size_t bytes = sizeof(double) * (size_t(kU) + 2 * kSplit + kFace);
 };
 
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(smem))),
-               "l"(gmem)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// Linear fifth-order upwind flux of one component: WENO with its weights
-// frozen at (0.1, 0.6, 0.3), on F+ at nodes face-3..face+1 (a..e) and on F-
-// mirrored (nodes face+2..face-2): (2a - 13b + 47c + 27d - 3e) / 60 each.
-template <typename T>
-__device__ __forceinline__ T linear_upwind(const T *P, const T *M, int ss) {
-  const T c0 = T(2.0 / 60.0), c1 = T(-13.0 / 60.0), c2 = T(47.0 / 60.0), c3 = T(27.0 / 60.0), c4 = T(-3.0 / 60.0);
-  const T plus = c0 * P[0] + c1 * P[ss] + c2 * P[2 * ss] + c3 * P[3 * ss] + c4 * P[4 * ss];
-  const T minus = c0 * M[4 * ss] + c1 * M[3 * ss] + c2 * M[2 * ss] + c3 * M[ss] + c4 * M[0];
-  return plus + minus;
-}
-
-// One tile (TI x TJ interior nodes starting at i0, j0) of one RK stage,
+// One FP64 tile (TI x TJ interior nodes starting at i0, j0) of one RK stage,
 // executed by all NT threads of a block; smem_raw holds StageSmem::bytes.
-// Shared by the per-solve kernel k_stage and the persistent batched kernel.
-// COH: the tile's inputs may have been written earlier in the same kernel by
-// other blocks (the persistent batched kernel): loads then go through L2
-// only (ld.global.cg) instead of the non-coherent read-only path, and U^n is
-// loaded in the epilogue instead of being prefetched with cp.async.
-template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false>
-__device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, const int i0, const int j0,
-                                           unsigned char *smem_raw) {
-  using S = StageSmem<T, TI, TJ>;
+// Every operation follows the reference's evaluation order (the unit is
+// compiled with -fmad=false).  Shared by the per-solve kernel k_stage and
+// the persistent batched kernel.  COH: the tile's inputs may have been
+// written earlier in the same kernel by other blocks (the persistent batched
+// kernel): loads then go through L2 only (ld.global.cg) instead of the
+// non-coherent read-only path.
+template <int SCHEME, int TI, int TJ, int NT, bool COH = false>
+__device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a, const int i0, const int j0,
+                                               unsigned char *smem_raw) {
+  using T = double;
+  using S = StageSmem<TI, TJ>;
   constexpr int HI = S::HI, HJ = S::HJ;
   T *Us = reinterpret_cast<T *>(smem_raw);
   T *Fp = Us + S::kU;
   T *Fm = Fp + S::kSplit;
   T *Hf = Fm + S::kSplit;
-  double *Uin64 = reinterpret_cast<double *>(smem_raw + sizeof(T) * (size_t(S::kU) + 2 * S::kSplit + S::kFace));
-  double *Un64 = Uin64 + 4 * TI * TJ;
-  // routed form: node flags of the tile with a 2-node halo, and the list of
-  // faces that need WENO
-  constexpr int FI = TI + 4, FJ = TJ + 4;
-  constexpr int kMaxFaces = (TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1);
-  __shared__ unsigned char sflag[ROUTE ? FI * FJ : 1];
-  __shared__ short slist[ROUTE ? kMaxFaces : 1];
-  __shared__ int scount;
-
-  constexpr bool F32 = sizeof(T) == 4;
-  const T gamma = F32 ? T(g.gamma32) : T(g.gamma);
-  const T zpl = F32 ? T(g.zpl32) : T(g.zp_lambda);
-
-  // FP32 form, stages 2 and 3: start fetching this tile's U^n now; it is
-  // needed only by the RK combination at the end.
-  [[maybe_unused]] const bool stage1 = a.a == 1.0 && a.b == 0.0 && a.un == a.uin;
-  if constexpr (F32 && !COH) {
-    if (a.mode == kModeRK && !stage1) {
-      for (int t = threadIdx.x; t < 4 * TI * TJ; t += NT) {
-        const int r = t / (TI * TJ), q = t - r * (TI * TJ);
-        const int i = q / TJ, j = q - (q / TJ) * TJ;
-        if (i0 + i < g.nx && j0 + j < g.ny)
-          cp_async8(&Un64[t], &a.un[r * g.plane + (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j)]);
-      }
-    }
-  }
+  const T gamma = g.gamma, zpl = g.zp_lambda;
 
   // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj.  All of a
   // thread's loads are issued before any is used, so they are in flight
@@ -119,26 +79,8 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
-      if (t < 4 * HI * HJ) {
-        if constexpr (F32) {
-          Us[t] = f64_to_f32(v[k]);  // integer ALU, not the FP64 pipe
-          const int r = t / (HI * HJ);
-          const int rem = t - r * (HI * HJ);
-          const int hi = rem / HJ, hj = rem - hi * HJ;
-          if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) Uin64[(r * TI + hi - 3) * TJ + hj - 3] = v[k];
-        } else {
-          Us[t] = v[k];
-        }
-      }
+      if (t < 4 * HI * HJ) Us[t] = v[k];
     }
-  }
-  if constexpr (ROUTE) {
-    for (int t = threadIdx.x; t < FI * FJ; t += NT) {
-      const int fi = t / FJ, fj = t - (t / FJ) * FJ;
-      const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;  // nodes i0-2+fi, j0-2+fj
-      sflag[t] = (ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
-    }
-    if (threadIdx.x == 0) scount = 0;
   }
   __syncthreads();
 
@@ -157,54 +99,25 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
   }
   __syncthreads();
   // x faces f = 0..TI: face between tile nodes f-1 and f (halo rows f+2, f+3)
-  if constexpr (ROUTE) {
-    for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
-      const int f = t / TJ, j = t - f * TJ;
-      if (i0 + f > g.nx || j0 + j >= g.ny) continue;
+  for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
+    const int f = t / TJ, j = t - f * TJ;
+    if (i0 + f > g.nx || j0 + j >= g.ny) continue;
+    T um[4], u0[4], out[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
-        Hf[(r * (TI + 1) + f) * TJ + j] = linear_upwind(Fp + (r * HI + f) * TJ + j, Fm + (r * HI + f + 1) * TJ + j, TJ);
-      // nodes f-2 .. f+1 of the tile = flag rows f .. f+3
-      const unsigned char *fl = sflag + f * FJ + (j + 2);
-      if (fl[0] | fl[FJ] | fl[2 * FJ] | fl[3 * FJ]) slist[atomicAdd(&scount, 1)] = short(t);
+    for (int r = 0; r < 4; ++r) {
+      um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
+      u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
     }
-    __syncthreads();
-    const int nw = scount;
-    for (int q = threadIdx.x; q < nw; q += NT) {
-      const int t = slist[q];
-      const int f = t / TJ, j = t - f * TJ;
-      T um[4], u0[4], out[4];
+    face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
-        u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
-      }
-      face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
-    }
-  } else {
-    for (int t = threadIdx.x; t < (TI + 1) * TJ; t += NT) {
-      const int f = t / TJ, j = t - f * TJ;
-      if (i0 + f > g.nx || j0 + j >= g.ny) continue;
-      T um[4], u0[4], out[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
-        u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
-      }
-      face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
-    }
+    for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
   }
   __syncthreads();
 
   // rhs = 0 + x term  (rhs zeroed in assembleRHS, then += in the x sweep)
   constexpr int PPT = (TI * TJ + NT - 1) / NT;
   T rhs[PPT][4];
-  const T dx = T(g.dx), dy = T(g.dy);
-  const T idx = T(g.inv_dx32), idy = T(g.inv_dy32);
+  const T dx = g.dx, dy = g.dy;
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -213,13 +126,9 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
     for (int r = 0; r < 4; ++r) {
       if (t < TI * TJ) {
         const T hr = Hf[(r * (TI + 1) + i + 1) * TJ + j], hl = Hf[(r * (TI + 1) + i) * TJ + j];
-        if constexpr (F32) rhs[k][r] = -(hr - hl) * idx;
-        else rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
+        rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
       }
     }
-  }
-  if constexpr (ROUTE) {
-    if (threadIdx.x == 0) scount = 0;
   }
   __syncthreads();
 
@@ -237,56 +146,23 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
     }
   }
   __syncthreads();
-  if constexpr (ROUTE) {
-    for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
-      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
-      if (i0 + i >= g.nx || j0 + f > g.ny) continue;
+  for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
+    const int i = t / (TJ + 1), f = t - i * (TJ + 1);
+    if (i0 + i >= g.nx || j0 + f > g.ny) continue;
+    T um[4], u0[4], out[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
-        Hf[(r * TI + i) * (TJ + 1) + f] = linear_upwind(Fp + (r * TI + i) * HJ + f, Fm + (r * TI + i) * HJ + f + 1, 1);
-      // nodes f-2 .. f+1 along y = flag columns f .. f+3 of flag row i+2
-      const unsigned char *fl = sflag + (i + 2) * FJ + f;
-      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount, 1)] = short(t);
+    for (int r = 0; r < 4; ++r) {
+      um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
+      u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
     }
-    __syncthreads();
-    const int nw = scount;
-    for (int q = threadIdx.x; q < nw; q += NT) {
-      const int t = slist[q];
-      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
-      T um[4], u0[4], out[4];
+    face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
-        u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
-      }
-      face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
-    }
-  } else {
-    for (int t = threadIdx.x; t < TI * (TJ + 1); t += NT) {
-      const int i = t / (TJ + 1), f = t - i * (TJ + 1);
-      if (i0 + i >= g.nx || j0 + f > g.ny) continue;
-      T um[4], u0[4], out[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
-        u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
-      }
-      face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
-#pragma unroll
-      for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
-    }
+    for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
   }
   __syncthreads();
 
   // --- y term, source, RK combination, store
   const double dt = COH ? __ldcg(a.dt) : *a.dt;
-  [[maybe_unused]] const double cdt = a.c * dt;
-  if constexpr (F32 && !COH) {
-    cp_async_wait_all();
-    __syncthreads();
-  }
 #pragma unroll
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
@@ -297,8 +173,7 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const T hr = Hf[(r * TI + i) * (TJ + 1) + j + 1], hl = Hf[(r * TI + i) * (TJ + 1) + j];
-      if constexpr (F32) rr[r] = rhs[k][r] - (hr - hl) * idy;
-      else rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
+      rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
     }
     const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
@@ -309,30 +184,21 @@ __device__ __forceinline__ void stage_tile(const Geom &g, const StageArgs &a, co
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const long long ix = r * g.plane + gidx;
-      if constexpr (F32) {
-        // FP64 RK combination from the staged FP64 values; stage 1
-        // (a = 1, b = 0, un == uin) is one FMA
-        const double rd = f32_to_f64(rr[r]);
-        const double ui = Uin64[(r * TI + i) * TJ + j];
-        if (a.mode == kModeRHS) a.uout[ix] = rd;
-        else if (stage1) a.uout[ix] = fma(cdt, rd, ui);
-        else if constexpr (COH) a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * __ldcg(&a.un[ix])));
-        else a.uout[ix] = fma(cdt, rd, fma(a.b, ui, a.a * Un64[(r * TI + i) * TJ + j]));
+      if (a.mode == kModeRHS) {
+        a.uout[ix] = rr[r];
       } else {
-        if (a.mode == kModeRHS) {
-          a.uout[ix] = double(rr[r]);
-        } else {
-          const double un = COH ? __ldcg(&a.un[ix]) : a.un[ix], ui = COH ? __ldcg(&a.uin[ix]) : a.uin[ix];
-          a.uout[ix] = a.a * un + a.b * ui + a.c * dt * double(rr[r]);
-        }
+        const double un = COH ? __ldcg(&a.un[ix]) : a.un[ix], ui = COH ? __ldcg(&a.uin[ix]) : a.uin[ix];
+        a.uout[ix] = a.a * un + a.b * ui + a.c * dt * rr[r];
       }
     }
   }
 }
 
-// The routed kernel asks for three resident blocks per SM: its per-face
-// characteristic-WENO path runs for a few percent of the faces, so trading
-// registers on that path for occupancy everywhere else pays.
+// Residency: the FP32 tiles read their FP64 inputs back in the epilogue
+// instead of staging them, and ask for four (routed) or three resident
+// 256-thread blocks per SM: the stage is issue-bound and latency-bound, and
+// trading registers for resident warps pays.  The FP64 tile is bound by the
+// FP64 pipe and keeps the registers.
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 && NT <= 256 ? (ROUTE ? 4 : 3) : 1) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
@@ -342,14 +208,14 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 && NT <= 256 ? (ROUTE ? 4 :
     stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, !(NT <= 256)>(
         g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x));
   else
-    stage_tile<T, SCHEME, TI, TJ, NT, ROUTE>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+    stage_tile_f64<SCHEME, TI, TJ, NT>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
 }
 
 // Dynamic shared memory of one stage tile.
 template <typename T, int TI, int TJ, bool ROUTE = false, int NT = 256>
 constexpr size_t stage_smem_bytes() {
   if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ, !(NT <= 256)>::bytes;
-  else return StageSmem<T, TI, TJ>::bytes;
+  else return StageSmem<TI, TJ>::bytes;
 }
 
 // Host-side launcher for one precision: picks the kernel instance for the
