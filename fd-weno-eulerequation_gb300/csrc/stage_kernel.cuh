@@ -199,13 +199,24 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
 // 256-thread blocks per SM: the stage is issue-bound and latency-bound, and
 // trading registers for resident warps pays.  The FP64 tile is bound by the
 // FP64 pipe and keeps the registers.
+template <typename T, bool ROUTE, int NT>
+__host__ __device__ constexpr int stage_blocks_per_sm() {
+  if constexpr (sizeof(T) == 8) return 1;
+  else return NT <= 256 ? (ROUTE ? 4 : 3) : (ROUTE ? 2 : 1);
+}
+// FP32 tiles stage their FP64 inputs in shared memory only at one block per SM.
+template <typename T, bool ROUTE, int NT>
+__host__ __device__ constexpr bool stage_keeps_inputs() {
+  return stage_blocks_per_sm<T, ROUTE, NT>() == 1;
+}
+
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 && NT <= 256 ? (ROUTE ? 4 : 3) : 1) k_stage(Geom g, StageArgs a) {
+__global__ void __launch_bounds__(NT, stage_blocks_per_sm<T, ROUTE, NT>()) k_stage(Geom g, StageArgs a) {
   if (*a.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // first interior node of the tile (0-based)
   if constexpr (sizeof(T) == 4)
-    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, !(NT <= 256)>(
+    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, stage_keeps_inputs<T, ROUTE, NT>()>(
         g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x));
   else
     stage_tile_f64<SCHEME, TI, TJ, NT>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
@@ -214,7 +225,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 && NT <= 256 ? (ROUTE ? 4 :
 // Dynamic shared memory of one stage tile.
 template <typename T, int TI, int TJ, bool ROUTE = false, int NT = 256>
 constexpr size_t stage_smem_bytes() {
-  if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ, !(NT <= 256)>::bytes;
+  if constexpr (sizeof(T) == 4) return StageSmem32<TI, TJ, stage_keeps_inputs<T, ROUTE, NT>()>::bytes;
   else return StageSmem<TI, TJ>::bytes;
 }
 
