@@ -701,6 +701,10 @@ int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float thres
   s->ind_logit_threshold = std::log(threshold / (1.0f - threshold));
   if (int rc = sync(s)) return rc;
   s->ind_ready = true;
+  // the time-loop graph holds the indicator launch and its threshold: capture
+  // it again on the next advance
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
   return WENOFD_OK;
 }
 

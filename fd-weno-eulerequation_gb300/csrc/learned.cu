@@ -337,7 +337,9 @@ __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A
   }
 }
 
-__global__ void __launch_bounds__(kCells, 8) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
+constexpr int kResident = 8;  // CTAs per SM: 28 KB shared memory, 64 registers, 64 TMEM columns each
+
+__global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
                                                             float logit_threshold, unsigned char *flags,
                                                             int flag_pitch, int *error, const int *active) {
   if (active && *active == 0) return;
@@ -531,7 +533,17 @@ void pack_indicator_weights(const float *params, void *host_out) {
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
                              unsigned char *flags, int *error, const int *active, cudaStream_t s) {
   const int tiles = ((g.nx + lrn::kTileI - 1) / lrn::kTileI) * ((g.ny + lrn::kTileJ - 1) / lrn::kTileJ);
-  const int grid = tiles < 152 * 8 ? tiles : 152 * 8;
+  // persistent CTAs: as many as are resident at once (tiles are dealt round
+  // robin, so a second wave would double the time): kResident per SM, the
+  // kernel's launch bound, which its shared memory, registers and tensor
+  // memory meet
+  static int sms_of[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int &sms = sms_of[dev & 63];
+  if (sms == 0 && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  const int grid = tiles < sms * lrn::kResident ? tiles : sms * lrn::kResident;
   lrn::k_indicator_tc<<<grid, lrn::kCells, 0, s>>>(g, U, static_cast<const lrn::IndicatorWeights *>(weights),
                                                    logit_threshold, flags, g.pitch, error, active);
   return cudaGetLastError();

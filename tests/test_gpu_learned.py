@@ -173,3 +173,28 @@ def test_learned_error_against_finer_reference_within_bound():
     elr = np.mean(np.abs(state_at(n, wenofd.LEARNED, params)[0] - fine[0]))
     print(f"L1 rho vs 2x finer FP64: plain FP64 {e64:.4e}, learned+FP32 {elr:.4e} (ratio {elr / e64:.3f})")
     assert elr <= 1.5 * e64
+
+
+def test_set_indicator_after_advance_takes_effect():
+    """advance() captures its time loop in a CUDA graph; loading (new)
+    indicator weights or a new threshold afterwards must reach the next
+    advance, as if the weights had been loaded before."""
+    p = _riemann_state(64, 48, 0, seed=5)
+    cfg = {"TESTCASE": 4, "ELEMNUMX": p.nx, "ELEMNUMY": p.ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1, "SEED": 5,
+           "PRECISION": wenofd.LEARNED}
+    P = mlp_oracle.init_params(3)
+    P[2720] = -1e4  # flags nothing: every face linear
+    with wenofd.Solver(cfg) as b:
+        b.initialize()
+        assert b.advance(max_steps=1) == 1  # no weights yet: every face WENO
+        U1, t1 = b.get_state(), b.info().now
+        b.set_indicator(P, 0.5)
+        assert b.advance(max_steps=2) == 2
+        Ub = b.get_state()
+    with wenofd.Solver(cfg) as e:
+        e.set_indicator(P, 0.5)
+        e.set_state(U1)
+        e.set_time(t1)
+        assert e.advance(max_steps=2) == 2
+        Ue = e.get_state()
+    assert np.array_equal(Ub, Ue)
