@@ -5,7 +5,9 @@
 Compiles every translation unit in parallel, skipping objects newer than
 their sources, into fd-weno-eulerequation_gb300/_build/.  The FP64 parity
 units are compiled with -fmad=false; host C++ with -ffp-contract=off so the
-initial conditions round like the reference's.
+initial conditions round like the reference's.  The FP32-arithmetic units
+(FP32 and learned forms, not bitwise by design) take the hardware square-root
+approximation (-prec-sqrt=false), the indicator also approximate division.
 """
 from __future__ import annotations
 
@@ -34,13 +36,13 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + 
 # translation unit -> extra flags
 CUDA_UNITS = {
     "stage_fp64.cu": ["-fmad=false"],
-    "stage_fp32.cu": [],
+    "stage_fp32.cu": ["-prec-sqrt=false"],
     "aux_kernels.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "learned_data.cu": ["-fmad=false"],
-    "learned.cu": [],
+    "learned.cu": ["-prec-sqrt=false", "-prec-div=false"],
     "batch_fp64.cu": ["-fmad=false"],
-    "batch_fp32.cu": [],
+    "batch_fp32.cu": ["-prec-sqrt=false"],
 }
 CXX_UNITS = ["capi.cpp", "cases.cpp", "batch.cpp"]
 

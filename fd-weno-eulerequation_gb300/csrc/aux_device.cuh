@@ -135,7 +135,7 @@ __device__ __forceinline__ void screen_speed(const Geom &g, double rho_d, double
     e = __int_as_float(0x7f800000);
     return;
   }
-  const float c = sqrtf(c2);
+  const float c = __fsqrt_rn(c2);
   const float au = fabsf(u), av = fabsf(v);
   s = __fadd_rn(__fmul_rn(__fadd_rn(au, c), g.inv_dx32), __fmul_rn(__fadd_rn(av, c), g.inv_dy32));
   const float rp = __fdiv_rn(__fmul_rn(__fmul_rn(12.0f, eps), __fadd_rn(fabsf(E), ke)), pp);

@@ -18,15 +18,16 @@ namespace dev {
 __device__ __forceinline__ float f64_to_f32(double d) {
   const unsigned hi = unsigned(__double2hiint(d));
   const unsigned lo = unsigned(__double2loint(d));
-  const unsigned sign = hi & 0x80000000u;
   const unsigned mag = hi & 0x7fffffffu;
-  // rebias the exponent inside the high word (1023 - 127 = 896), then move
-  // exponent and the top 20 mantissa bits up by 3 and append 3 more
-  const unsigned bits = sign | ((mag - 0x38000000u) << 3) | (lo >> 29);
-  if (mag < 0x38100000u) return __uint_as_float(sign);  // zero, subnormal, below 2^-126
-  if (mag >= 0x47f00000u) {                             // beyond FP32 range, inf, NaN
+  // (hi, lo) << 3 keeps the low 9 exponent bits and the top 23 mantissa bits
+  // in place for FP32; subtracting 0x180 << 23 rebiases the exponent
+  // (1023 - 127 = 896 = 0x380, congruent to 0x180 modulo 2^9), which leaves
+  // bit 31 clear for every in-range magnitude; the sign is put back.
+  const unsigned bits = (__funnelshift_l(lo, hi, 3) - 0xC0000000u) | (hi & 0x80000000u);
+  if (mag < 0x38100000u) return __uint_as_float(hi & 0x80000000u);  // zero, subnormal, below 2^-126
+  if (mag >= 0x47f00000u) {                                           // beyond FP32 range, inf, NaN
     const bool nan = mag > 0x7ff00000u || (mag == 0x7ff00000u && lo != 0u);
-    return __uint_as_float(sign | 0x7f800000u | (nan ? 0x400000u : 0u));
+    return __uint_as_float((hi & 0x80000000u) | 0x7f800000u | (nan ? 0x400000u : 0u));
   }
   return __uint_as_float(bits);
 }

@@ -15,6 +15,8 @@ namespace wenofd {
 namespace dev {
 
 __device__ __forceinline__ double tsqrt(double x) { return sqrt(x); }
+// FP32: the units of the FP32 forms are compiled with -prec-sqrt=false, so
+// this is the hardware approximation there (about 1 ulp).
 __device__ __forceinline__ float tsqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double tabs(double x) { return fabs(x); }
 __device__ __forceinline__ float tabs(float x) { return fabsf(x); }
