@@ -226,6 +226,7 @@ __global__ void k_advance_setup(Ctrl *c, long long max_steps) {
   c->screen_bits = 0u;
   c->nan_flag = 0;
   c->bounds_valid = 0;
+  c->ind_base = c->steps;
 }
 
 __global__ void k_copy_interior(Geom g, const double *src, double *dst, const int *active) {

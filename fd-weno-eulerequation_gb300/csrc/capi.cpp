@@ -105,8 +105,9 @@ int sync(wenofd_solver *s) {
 
 // bounds: this stage writes U^{n+1} at the end of a graph-driven step; its
 // epilogue also screens the next time step (FP32 forms).
+// timeloop: launched by the graph-driven step of wenofd_advance.
 int launch_stage(wenofd_solver *s, const double *in, const double *un, double *out, double a, double b,
-                 double c, int mode, bool bounds = false) {
+                 double c, int mode, bool bounds = false, bool timeloop = false) {
   StageArgs args;
   args.uin = in;
   args.un = un;
@@ -128,7 +129,8 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   // input (ghosts just filled); all stages of the step route with those flags.
   if (s->precision == WENOFD_LEARNED && in == s->S && un == s->S && s->ind_ready) {
     CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
-                                      &s->ctrl->active, s->stream));
+                                      &s->ctrl->active, timeloop ? s->ctrl : nullptr, s->ind_interval,
+                                      s->stream));
     s->launches += 1;
   }
   if (s->precision != WENOFD_FP64) {
@@ -143,20 +145,20 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
 // reads its input with a halo and writes a different buffer; the last stage
 // writes U^{n+1} over U^n, which it reads only at the node itself.
 // fused: the last stage also screens the next time step (RK2, RK3).
-int enqueue_rk(wenofd_solver *s, bool fused = false) {
+int enqueue_rk(wenofd_solver *s, bool fused = false, bool timeloop = false) {
   int rc;
   double *S = s->S, *A = s->A, *B = s->B;
   switch (s->rk) {
     case 0:  // U += dt * rhs, as (1*U + 0*U) + (1*dt)*rhs (same rounding)
-      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK, false, timeloop))) return rc;
       CUDA_TRY(wenofd::launch_copy_interior(s->g, A, S, &s->ctrl->active, s->stream));
       s->launches += 1;
       return WENOFD_OK;
     case 1:
-      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK, false, timeloop))) return rc;
       return launch_stage(s, A, S, S, 0.5, 0.5, 0.5, wenofd::kModeRK, fused);
     case 2:
-      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK))) return rc;
+      if ((rc = launch_stage(s, S, S, A, 1.0, 0.0, 1.0, wenofd::kModeRK, false, timeloop))) return rc;
       if ((rc = launch_stage(s, A, S, B, 3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0, wenofd::kModeRK))) return rc;
       return launch_stage(s, B, S, S, 1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0, wenofd::kModeRK, fused);
   }
@@ -182,7 +184,7 @@ int enqueue_step(wenofd_solver *s) {
   if (int rc = enqueue_dt_reduce(s)) return rc;
   CUDA_TRY(wenofd::launch_dt_finalize(s->ctrl, s->stream));
   const bool fused = s->tile_bounds && s->rk != 0;
-  int rc = enqueue_rk(s, fused);
+  int rc = enqueue_rk(s, fused, true);
   if (rc) return rc;
   CUDA_TRY(wenofd::launch_step_end(s->ctrl, fused ? 1 : 0, s->stream));
   s->launches += 3;
@@ -256,6 +258,9 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   double label_deviation = 1e-2;
   if (!get_double(opt, "LABEL_DEVIATION", label_deviation, false) || !(label_deviation > 0.0))
     return fail(WENOFD_BAD_CONFIG, "bad LABEL_DEVIATION");
+  int ind_interval = 1;
+  if (!get_int(opt, "INDICATOR_INTERVAL", ind_interval, false) || ind_interval < 1 || ind_interval > 1000)
+    return fail(WENOFD_BAD_CONFIG, "bad INDICATOR_INTERVAL");
   {
     auto it = opt.find("SEED");
     if (it != opt.end()) {
@@ -312,6 +317,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   s->tile_i = tile_i;
   s->cfl = cfl;
   s->label_deviation = label_deviation;
+  s->ind_interval = ind_interval;
   s->cs = cs;
   const double dx = (cs.xr - cs.xl) / (nx - 1);  // src/WENOFD.cpp:73-74
   const double dy = (cs.yr - cs.yl) / (ny - 1);
@@ -708,6 +714,16 @@ int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float thres
   return WENOFD_OK;
 }
 
+int wenofd_routing_flags(wenofd_solver *s, unsigned char *host_flags) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_flags) return fail(WENOFD_BAD_ARG, "null flags");
+  if (s->precision != WENOFD_LEARNED) return fail(WENOFD_BAD_CONFIG, "routing flags need PRECISION = 2");
+  CUDA_TRY(cudaSetDevice(s->device));
+  CUDA_TRY(cudaMemcpy2DAsync(host_flags, s->ny, s->flags + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost,
+                             s->g.pitch, s->ny, s->nx, cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
 int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
   if (int rc = check_handle(s)) return rc;
   if (!host_flags) return fail(WENOFD_BAD_ARG, "null flags");
@@ -717,7 +733,7 @@ int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
   CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
   CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
-                                    nullptr, s->stream));
+                                    nullptr, nullptr, 1, s->stream));
   s->launches += 3;
   CUDA_TRY(cudaMemcpy2DAsync(host_flags, s->ny, s->flags + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost,
                              s->g.pitch, s->ny, s->nx, cudaMemcpyDeviceToHost, s->stream));

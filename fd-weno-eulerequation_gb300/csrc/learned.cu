@@ -341,8 +341,10 @@ constexpr int kResident = 8;  // CTAs per SM: 28 KB shared memory, 64 registers,
 
 __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
                                                             float logit_threshold, unsigned char *flags,
-                                                            int flag_pitch, int *error, const int *active) {
+                                                            int flag_pitch, int *error, const int *active,
+                                                            const Ctrl *ctrl, int interval) {
   if (active && *active == 0) return;
+  if (ctrl && interval > 1 && (ctrl->steps - ctrl->ind_base) % interval != 0) return;
   __shared__ __align__(128) __nv_bfloat16 sA[kCells * kK1];  // A1, then A2 [128 x 48] (and the layer-3 input)
   __nv_bfloat16 *const sA1 = sA, *const sA2 = sA;
   __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
@@ -531,7 +533,8 @@ void pack_indicator_weights(const float *params, void *host_out) {
 }
 
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
-                             unsigned char *flags, int *error, const int *active, cudaStream_t s) {
+                             unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
+                             cudaStream_t s) {
   const int tiles = ((g.nx + lrn::kTileI - 1) / lrn::kTileI) * ((g.ny + lrn::kTileJ - 1) / lrn::kTileJ);
   // persistent CTAs: as many as are resident at once (tiles are dealt round
   // robin, so a second wave would double the time): kResident per SM, the
@@ -545,7 +548,8 @@ cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights
   if (sms == 0 && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
   const int grid = tiles < sms * lrn::kResident ? tiles : sms * lrn::kResident;
   lrn::k_indicator_tc<<<grid, lrn::kCells, 0, s>>>(g, U, static_cast<const lrn::IndicatorWeights *>(weights),
-                                                   logit_threshold, flags, g.pitch, error, active);
+                                                   logit_threshold, flags, g.pitch, error, active, ctrl,
+                                                   interval);
   return cudaGetLastError();
 }
 

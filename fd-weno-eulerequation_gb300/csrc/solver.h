@@ -32,6 +32,7 @@ struct wenofd_solver {
   int *ind_error = nullptr;
   float ind_logit_threshold = 0.0f;
   double label_deviation = 1e-2;  // LABEL_DEVIATION: training-label threshold
+  int ind_interval = 1;            // INDICATOR_INTERVAL: steps per indicator run in the time loop
   bool ind_ready = false;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;

@@ -48,6 +48,9 @@ struct Ctrl {
   // in screen_bits) are valid, so the time-step reduction skips its screen
   // pass.  Cleared at the start of every advance and by every other entry.
   int bounds_valid;
+  // Learned form: steps counted from here (set at the start of every
+  // advance) decide which steps run the indicator (INDICATOR_INTERVAL).
+  long long ind_base;
 };
 
 // Arguments of one RK stage launch.  uin is read with a 3-node halo (its
@@ -136,8 +139,12 @@ void pack_indicator_weights(const float *params, void *host_out);
 cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStream_t s);
 // labels: 1 where a face of the node has a WENO-Z weight deviation above `deviation`
 cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, double deviation, cudaStream_t s);
+// With ctrl set (the time loop), the indicator runs only on steps whose
+// count since Ctrl::ind_base is a multiple of `interval`; the flags of the
+// last run route the steps in between.
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
-                             unsigned char *flags, int *error, const int *active, cudaStream_t s);
+                             unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
+                             cudaStream_t s);
 
 // aux_kernels.cu
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s);

@@ -91,6 +91,7 @@ def lib() -> C.CDLL:
         VP = C.c_void_p
         L.wenofd_set_indicator.argtypes = [H, C.POINTER(C.c_float), C.c_float]
         L.wenofd_indicator_flags.argtypes = [H, C.POINTER(C.c_ubyte)]
+        L.wenofd_routing_flags.argtypes = [H, C.POINTER(C.c_ubyte)]
         L.wenofd_indicator_data.argtypes = [H, VP, VP]
         L.wenofd_mlp_forward.argtypes = [VP, VP, C.c_longlong, VP, VP]
         L.wenofd_mlp_backward.argtypes = [VP, VP, VP, C.c_longlong, VP, VP, VP]
@@ -115,7 +116,8 @@ def lib() -> C.CDLL:
                   "wenofd_step", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_set_state_device",
                   "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
                   "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
-                  "wenofd_set_indicator", "wenofd_indicator_flags", "wenofd_indicator_data", "wenofd_mlp_forward",
+                  "wenofd_set_indicator", "wenofd_indicator_flags", "wenofd_routing_flags", "wenofd_indicator_data",
+                  "wenofd_mlp_forward",
                   "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train"):
             getattr(L, f).restype = C.c_int
         _lib = L
@@ -261,6 +263,12 @@ class Solver:
         _check(lib().wenofd_indicator_flags(self._h, out.ctypes.data_as(C.POINTER(C.c_ubyte))))
         return out
 
+    def routing_flags(self) -> np.ndarray:
+        """The stored flags that routed the last step (no indicator run)."""
+        out = np.zeros((self.nx, self.ny), dtype=np.uint8)
+        _check(lib().wenofd_routing_flags(self._h, out.ctypes.data_as(C.POINTER(C.c_ubyte))))
+        return out
+
     def indicator_data(self, dev_features: int | None, dev_labels: int | None) -> None:
         """Features [NX*NY][50] float32 / labels [NX*NY] uint8 into device buffers."""
         _check(lib().wenofd_indicator_data(self._h, C.c_void_p(dev_features or 0), C.c_void_p(dev_labels or 0)))
@@ -324,6 +332,7 @@ EXPORTED = [
     "wenofd_fill_boundary", "wenofd_get_flux", "wenofd_calc_dt", "wenofd_rk_step", "wenofd_step",
     "wenofd_advance", "wenofd_error_norms", "wenofd_conservation_sums", "wenofd_time_stages",
     "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values", "wenofd_set_indicator", "wenofd_indicator_flags",
+    "wenofd_routing_flags",
     "wenofd_indicator_data", "wenofd_mlp_forward", "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train",
     "wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
     "wenofd_batch_advance", "wenofd_batch_get_info",

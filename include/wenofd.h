@@ -77,7 +77,8 @@ const char *wenofd_version(void);
  * 2 learned + FP32), SEED (seeded cases), TEND (overrides
  * equation->outputtime), DEVICE, TILE_I (stage-kernel tile height; 0 =
  * default), LABEL_DEVIATION (training labels of wenofd_indicator_data;
- * default 1e-2), and overrides of the
+ * default 1e-2), INDICATOR_INTERVAL (time steps per indicator run, see
+ * wenofd_routing_flags; default 1), and overrides of the
  * EulerEquation members the reference's callers may set on their equation
  * object (utils/equations.hpp:58-70): XL, XR, YL, YR, GAMMA, BC_LEFT,
  * BC_RIGHT, BC_BOTTOM, BC_TOP (BOUNDARYTYPE values), GRAVITY (0/1). */
@@ -161,8 +162,15 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch);
  * cores) into a PRECISION = 2 solver; nodes whose predicted probability
  * exceeds `threshold` are flagged.  Without it every face takes WENO. */
 int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float threshold);
-/* Run the indicator on the current state; flags [NX][NY] bytes to the host. */
+/* Run the indicator on the current state; flags [NX][NY] bytes to the host
+ * (they also become the stored routing flags). */
 int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags);
+/* The stored routing flags [NX][NY] as they are (no indicator run): those of
+ * the indicator's last run, which routed the last step.  In the time loop
+ * the indicator runs on the first step of every wenofd_advance call and then
+ * on every INDICATOR_INTERVAL-th step (config key, default 1); the steps in
+ * between route with the flags of its last run. */
+int wenofd_routing_flags(wenofd_solver *s, unsigned char *host_flags);
 /* Training data of the current state: features [NX*NY][50] float and labels
  * [NX*NY] bytes (1 where WENO-Z's nonlinear weights differ from the linear
  * ones by more than LABEL_DEVIATION, default 1e-2, on a non-flat stencil at

@@ -198,3 +198,33 @@ def test_set_indicator_after_advance_takes_effect():
         assert e.advance(max_steps=2) == 2
         Ue = e.get_state()
     assert np.array_equal(Ub, Ue)
+
+
+@pytest.mark.parametrize("interval", [1, 2, 3])
+def test_indicator_interval_in_the_time_loop(interval):
+    """INDICATOR_INTERVAL = k: inside one advance call the indicator runs on
+    steps 0, k, 2k, ... and the steps between route with its last flags.
+    After an advance of `steps` steps the stored flags are the indicator's
+    output on the state at the last step it ran."""
+    steps = 4
+    P = mlp_oracle.init_params(7)
+    cfg = {"TESTCASE": 4, "ELEMNUMX": 80, "ELEMNUMY": 64, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1, "SEED": 6,
+           "PRECISION": wenofd.LEARNED, "INDICATOR_INTERVAL": interval}
+
+    def run(n):
+        with wenofd.Solver(cfg) as s:
+            s.initialize()
+            s.set_indicator(P, 0.5)
+            if n:
+                assert s.advance(max_steps=n) == n
+            return s.get_state(), s.routing_flags()
+
+    _, stored = run(steps)
+    last_run = ((steps - 1) // interval) * interval
+    U, _ = run(last_run)  # the state at the start of that step
+    with wenofd.Solver(cfg) as q:
+        q.set_indicator(P, 0.5)
+        q.set_state(U)
+        want = q.indicator_flags()
+    assert np.array_equal(stored, want)
+    assert 0.0 < want.mean() < 1.0
