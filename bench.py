@@ -456,6 +456,20 @@ def main() -> None:
     torch.cuda.synchronize(local)
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e_value = world * k_e2e * cells / e2e_s
+    # the reference's usage, CWENOFD::run: the state in once, the time loop,
+    # the state out once (here over the bench's step count)
+    barrier()
+    torch.cuda.synchronize(local)
+    t0 = time.perf_counter()
+    sl.set_state_ptr(host.data_ptr())
+    assert sl.advance(max_steps=args.steps) == args.steps
+    sl.get_state_ptr(host.data_ptr())
+    torch.cuda.synchronize(local)
+    run_s = max_over_ranks(time.perf_counter() - t0)
+    e2e_run = {"value": world * args.steps * cells / run_s, "unit": "cell-updates/s", "steps": args.steps,
+               "h2d_bytes": 4 * cells * 8, "d2h_bytes": 4 * cells * 8,
+               "path": "C ABI wenofd_set_state + wenofd_advance(steps) + wenofd_get_state, pinned host "
+                       "(the state crosses once each way per run, as CWENOFD::run)"}
     sl.close()
 
     # ---- batching: many uneven solves in one persistent launch vs one at a time
@@ -499,6 +513,7 @@ def main() -> None:
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "steps": k_e2e,
                     "h2d_bytes_per_step": 4 * cells * 8, "d2h_bytes_per_step": 4 * cells * 8,
                     "path": "C ABI wenofd_set_state + wenofd_advance(1) + wenofd_get_state, pinned host"},
+            "e2e_run": e2e_run,
             "clocks": clocks,
             "batching": batching,
         }
