@@ -207,49 +207,65 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     }
   }
 
-  // --- state tile with halo, one node (four components) per thread and
-  // item: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).  All loads of a
-  // thread (state, and the routed form's node flags: tile + 2-node halo,
-  // flag node (fi, fj) = global (2 + i0 + fi, 2 + j0 + fj)) are issued
+  // --- state tile with halo: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).
+  // A thread loads a pair of adjacent nodes per component with one 128-bit
+  // load: pair p of halo row hi covers global columns j0 + 2p and j0 + 2p + 1
+  // (16-byte aligned: rows start on 256-byte boundaries, j0 is even), i.e.
+  // hj = 2p - 1 and 2p; 20 pairs span the 38 halo columns (the first and last
+  // loaded node are not needed).  The routed form's node flags (tile + 2-node
+  // halo, flag node (fi, fj) = global (2 + i0 + fi, 2 + j0 + fj)) come as
+  // aligned 32-bit words the same way.  All loads of a thread are issued
   // before any is used.
   {
-    constexpr int NLD = (HI * HJ + NT - 1) / NT;
-    constexpr int NFL = ROUTE ? (FI * FJ + NT - 1) / NT : 1;
-    double v[NLD][4];
-    unsigned char fv[NFL];
+    constexpr int PJ = (HJ + 2) / 2;  // pairs per halo row
+    constexpr int NLD = (HI * PJ + NT - 1) / NT;
+    constexpr int WJ = (FJ + 2 + 3) / 4;  // flag words per row: global columns j0 .. j0 + 4 WJ - 1
+    constexpr int NFL = ROUTE ? (FI * WJ + NT - 1) / NT : 1;
+    double2 v[NLD][4];
+    unsigned fv[NFL];
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
-      const int hi = t / HJ, hj = t - (t / HJ) * HJ;
-      const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
-      const bool ok = t < HI * HJ && ei < g.nxt && ej < g.nyt;
-      const double *src = a.uin + (long long)ei * g.pitch + ej;
+      const int hi = t / PJ, p = t - (t / PJ) * PJ;
+      const int ei = 1 + i0 + hi, ej = j0 + 2 * p;
+      const bool ok = t < HI * PJ && ei < g.nxt && ej < g.pitch;
+      const double2 *src = reinterpret_cast<const double2 *>(a.uin + (long long)ei * g.pitch + ej);
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        if constexpr (COH) v[k][r] = ok ? __ldcg(src + r * g.plane) : 0.0;
-        else v[k][r] = ok ? __ldg(src + r * g.plane) : 0.0;
+        if constexpr (COH) v[k][r] = ok ? __ldcg(src + r * (g.plane / 2)) : make_double2(0.0, 0.0);
+        else v[k][r] = ok ? __ldg(src + r * (g.plane / 2)) : make_double2(0.0, 0.0);
       }
     }
     if constexpr (ROUTE) {
 #pragma unroll
       for (int k = 0; k < NFL; ++k) {
         const int t = threadIdx.x + k * NT;
-        const int fi = t / FJ, fj = t - (t / FJ) * FJ;
-        const int ei = 2 + i0 + fi, ej = 2 + j0 + fj;
-        fv[k] = (t < FI * FJ && ei < g.nxt && ej < g.nyt) ? a.flags[(long long)ei * g.pitch + ej] : 1;
+        const int fi = t / WJ, w = t - (t / WJ) * WJ;
+        const int ei = 2 + i0 + fi, ej = j0 + 4 * w;
+        fv[k] = (t < FI * WJ && ei < g.nxt && ej < g.pitch)
+                    ? *reinterpret_cast<const unsigned *>(a.flags + (long long)ei * g.pitch + ej)
+                    : 0x01010101u;
       }
     }
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
-      if (t < HI * HJ) {
-        Us[t] = make_float4(f64_to_f32(v[k][0]), f64_to_f32(v[k][1]), f64_to_f32(v[k][2]), f64_to_f32(v[k][3]));
-        const int hi = t / HJ, hj = t - (t / HJ) * HJ;
-        if constexpr (KEEP) {
-          if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
-            const int q = (hi - 3) * TJ + hj - 3;
+      if (t < HI * PJ) {
+        const int hi = t / PJ, p = t - (t / PJ) * PJ;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = v[k][r];
+        for (int h = 0; h < 2; ++h) {
+          const int hj = 2 * p - 1 + h;
+          if (hj < 0 || hj >= HJ) continue;
+          double x[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) x[r] = h ? v[k][r].y : v[k][r].x;
+          Us[hi * HJ + hj] = make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
+          if constexpr (KEEP) {
+            if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
+              const int q = (hi - 3) * TJ + hj - 3;
+#pragma unroll
+              for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = x[r];
+            }
           }
         }
       }
@@ -258,7 +274,14 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
 #pragma unroll
       for (int k = 0; k < NFL; ++k) {
         const int t = threadIdx.x + k * NT;
-        if (t < FI * FJ) sflag[t] = fv[k];
+        if (t < FI * WJ) {
+          const int fi = t / WJ, w = t - (t / WJ) * WJ;
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int fj = 4 * w + c - 2;  // global column j0 + 4w + c = 2 + j0 + fj
+            if (fj >= 0 && fj < FJ) sflag[fi * FJ + fj] = (unsigned char)(fv[k] >> (8 * c));
+          }
+        }
       }
       if (threadIdx.x == 0) scount = 0;
     }
