@@ -248,13 +248,15 @@ def finer_reference_errors(wenofd, params, device: int, n: int = 513, t_end: flo
     return e
 
 def errors_at_t1(wenofd, params, device: int, n: int = 513) -> dict:
-    """Density of the FP32 and learned forms against the FP64 path (bitwise
-    the reference) on the same grid after the whole run to t = 1: shear
-    layer, seed SEED, n^2."""
+    """Density after the whole run to t = 1 (shear layer, seed SEED): the
+    FP32 and learned forms against the FP64 path (bitwise the reference) on
+    the same n^2 grid, and, because the layer has rolled up by then and the
+    flow is sensitive to any perturbation, plain FP64 and the learned form at
+    ((n+1)/2)^2 against that n^2 FP64 solution (fine node 2k = coarse node k)."""
     import numpy as np
 
-    def state_at(prec, par=None):
-        cfg = dict(config_for(prec, device), ELEMNUMX=n, ELEMNUMY=n, TEND=1.0)
+    def state_at(m, prec, par=None):
+        cfg = dict(config_for(prec, device), ELEMNUMX=m, ELEMNUMY=m, TEND=1.0)
         with wenofd.Solver(cfg) as s:
             s.initialize()
             if par is not None:
@@ -262,11 +264,17 @@ def errors_at_t1(wenofd, params, device: int, n: int = 513) -> dict:
             steps = s.advance(-1)
             return s.get_state()[0], steps
 
-    rho64, steps = state_at(wenofd.FP64)
+    rho64, steps = state_at(n, wenofd.FP64)
     out = {"setup": f"shear layer {n}^2 to t = 1 ({steps} RK3 steps), density vs the FP64 path on the same grid"}
     for name, prec, par in (("fp32", wenofd.FP32, None), ("learned_fp32", wenofd.LEARNED, params)):
-        d = state_at(prec, par)[0] - rho64
+        d = state_at(n, prec, par)[0] - rho64
         out[name] = {"l1": float(np.mean(np.abs(d))), "linf": float(np.max(np.abs(d)))}
+    m = (n + 1) // 2
+    fine = rho64[::2, ::2]
+    e64 = float(np.mean(np.abs(state_at(m, wenofd.FP64)[0] - fine)))
+    elr = float(np.mean(np.abs(state_at(m, wenofd.LEARNED, params)[0] - fine)))
+    out["vs_2x_finer_fp64"] = {"setup": f"{m}^2 vs the {n}^2 FP64 solution at t = 1", "fp64": e64,
+                               "learned_fp32": elr, "ratio_learned_to_fp64": elr / e64}
     return out
 
 
