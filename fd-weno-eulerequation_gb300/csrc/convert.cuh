@@ -51,5 +51,18 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   return __hiloint2double(int(hi), int(lo));
 }
 
+// x * 2^-K on the integer ALU: exact, except that results that would be
+// subnormal (below 2^-1022 in magnitude) become signed zero; infinity and NaN
+// pass through.
+template <int K>
+__device__ __forceinline__ double scale_pow2_down(double x) {
+  static_assert(K >= 1 && K < 16, "small power-of-two scales only");
+  const unsigned hi = unsigned(__double2hiint(x));
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e == 0x7ffu) return x;
+  if (e <= unsigned(K)) return __hiloint2double(int(hi & 0x80000000u), 0);
+  return __hiloint2double(int(hi - (unsigned(K) << 20)), __double2loint(x));
+}
+
 }  // namespace dev
 }  // namespace wenofd

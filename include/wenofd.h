@@ -139,7 +139,11 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
  * against the exact solution at the current time: out = {Linf, L1, L2},
  * L1/L2 normalised by NX*NY.  FP64 device reduction. */
 int wenofd_error_norms(wenofd_solver *s, double out[3]);
-/* Interior sums of rho, rho*u, rho*v, E (FP64 device reduction). */
+/* Interior sums of rho, rho*u, rho*v, E over all NX*NY nodes (FP64 device
+ * reduction).  The grid is node-based: in a periodic direction the last node
+ * duplicates the first, so these sums move by the duplicate row's change;
+ * the conserved totals run over the unique nodes (drop the last row and
+ * column of the state). */
 int wenofd_conservation_sums(wenofd_solver *s, double out[4]);
 
 /* Measurement aid, no reference counterpart: replays the RK stage kernels of
