@@ -193,6 +193,46 @@ def time_form(wenofd, torch, precision: int, device: int, steps: int, warmup: in
     return s, ms, launches
 
 
+def kernel_tour(wenofd, torch, device: int, n: int) -> dict:
+    """Every kernel of the path once, untimed, at n^2 (shear layer): the plain
+    FP64 and FP32 forms one RK3 step each with their time-step reductions and
+    conservation sums; one FP64 WENO-JS step of the smooth wave and its
+    density error norms; the learned form's data
+    extraction, one training epoch on that data, and one step with the
+    trained indicator; one step of a two-member FP32 and FP64 batch."""
+    from wenofd import learned
+
+    ran = {}
+    for name, prec in (("fp64", wenofd.FP64), ("fp32", wenofd.FP32)):
+        with wenofd.Solver(dict(config_for(prec, device), ELEMNUMX=n, ELEMNUMY=n)) as s:
+            s.initialize()
+            ran[name] = {"steps": s.advance(max_steps=1), "mass": float(s.conservation_sums()[0])}
+    with wenofd.Solver({"TESTCASE": 0, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.05, "SCHEME": 0,
+                        "DEVICE": device}) as s:  # smooth wave: the error norms against its exact solution
+        s.initialize()
+        ran["wave_fp64"] = {"steps": s.advance(max_steps=1), "l1": float(s.error_norms()[1])}
+    X, y = learned.generate_dataset(torch, runs=((5, 11),), n=n, snapshots=(2,), per_snapshot=32768,
+                                    device=device, label_deviation=LABEL_DEVIATION)
+    params, losses = learned.train(torch, X, y, epochs=1, batch=4096, lr=3e-3)
+    with wenofd.Solver(dict(config_for(wenofd.LEARNED, device), ELEMNUMX=n, ELEMNUMY=n)) as s:
+        s.initialize()
+        s.set_indicator(params, THRESHOLD)
+        ran["learned"] = {"steps": s.advance(max_steps=1), "flagged": float(s.indicator_flags().mean()),
+                          "samples": int(len(y)), "loss": float(losses[0])}
+    for name, prec in (("batch_fp32", wenofd.FP32), ("batch_fp64", wenofd.FP64)):
+        members = [wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": m, "ELEMNUMY": m, "RKMETH": 2, "CFL": 0.7,
+                                  "SCHEME": 1, "SEED": 1000 + m, "PRECISION": prec, "DEVICE": device})
+                   for m in (128, 256)]
+        for s in members:
+            s.initialize()
+        with wenofd.Batch(members) as b:
+            ran[name] = {"steps": b.advance(max_steps=1)}
+        for s in members:
+            s.close()
+    torch.cuda.synchronize(device)
+    return ran
+
+
 def train_indicator(torch, device: int):
     """The indicator is trained on the GPU before timing: solver-produced
     stencils (two shear layers, two Riemann problems, seeds != SEED, 512^2,
@@ -384,6 +424,8 @@ def main() -> None:
                     help="time the FP32 form only (no training, no other legs): for profiling")
     ap.add_argument("--only-headline", action="store_true",
                     help="time the headline form only (no other legs, errors, e2e or CPU leg): for profiling")
+    ap.add_argument("--kernel-tour", type=int, default=0, metavar="N",
+                    help="run every kernel of the path once at N^2, untimed, and exit: for per-kernel counters")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -422,6 +464,11 @@ def main() -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.kernel_tour:
+        ran = kernel_tour(wenofd, torch, local, args.kernel_tour)
+        if rank == 0:
+            print(json.dumps({"kernel_tour": ran, "n": args.kernel_tour, "note": "untimed (profiling run)"}))
+        return
     if args.only_fp32:
         s32, ms32, launches = time_form(wenofd, torch, wenofd.FP32, local, args.steps, args.warmup, stream)
         s32.close()

@@ -33,10 +33,12 @@ __global__ void k_dt_reduce(Geom g, const double *U, Ctrl *c) {
   const double gamma = g.gamma;
   double smax = 0.0;
   int nan_seen = 0;
+  dev::SpeedMemo memo;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
     const long long base = (long long)(kGhost + i) * g.pitch + (kGhost + j);
     const double rho = U[base], mu = U[g.plane + base], mv = U[2 * g.plane + base], E = U[3 * g.plane + base];
+    if (memo.repeat(rho, mu, mv, E)) continue;
     const double u = mu / rho, v = mv / rho;
     const double p = (gamma - 1.0) * (E - 0.5 * rho * (u * u + v * v));
     const double cs = sqrt(gamma * p / rho);
@@ -103,12 +105,13 @@ __global__ void k_dt_refine(Geom g, const double *U, Ctrl *c, const float2 *boun
   const float L = __uint_as_float(c->screen_bits);
   double smax = 0.0;
   int nan_seen = 0;
+  dev::SpeedMemo memo;
   auto visit = [&](int i, int j) {
     const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
     const double rho = U[b], mu = U[g.plane + b], mv = U[2 * g.plane + b], E = U[3 * g.plane + b];
     float s32, e;
     dev::screen_speed(g, rho, mu, mv, E, s32, e);
-    if (s32 + e >= L) {
+    if (s32 + e >= L && !memo.repeat(rho, mu, mv, E)) {
       const double s = dev::exact_speed(g, rho, mu, mv, E);
       if (s != s) nan_seen = 1;
       else if (s > smax) smax = s;

@@ -204,6 +204,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
       if constexpr (F32) L = __uint_as_float(__ldcg(&M.ctrl->screen_bits));
       double smax = 0.0;
       int nan_seen = 0;
+      SpeedMemo memo;
       for (long long t = first + threadIdx.x; t < first + kPtChunk && t < npts; t += NT) {
         double rho, mu, mv, E;
         node(M, t, rho, mu, mv, E);
@@ -212,6 +213,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
           screen_speed(M.g, rho, mu, mv, E, s32, e);
           if (!(s32 + e >= L)) continue;
         }
+        if (memo.repeat(rho, mu, mv, E)) continue;
         const double s = exact_speed(M.g, rho, mu, mv, E);
         if (s != s) nan_seen = 1;
         else if (s > smax) smax = s;
