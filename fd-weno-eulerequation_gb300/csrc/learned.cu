@@ -317,13 +317,31 @@ __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A
                                              float tail1) {
   constexpr int kc = kK1 / 8;
   const float c = w[12];
+  // differences and scaling on packed FP32 pairs (two operations per
+  // instruction); a flat window scales by 0, which gives the GEMM the same
+  // zero inputs as the explicit zeros of the training-side features
+  float d[26];
+#pragma unroll
+  for (int k = 0; k < 24; k += 2) {
+    const float2 q = __fadd2_rn(make_float2(w[k], w[k + 1]), make_float2(-c, -c));
+    d[k] = q.x;
+    d[k + 1] = q.y;
+  }
+  d[24] = w[24] - c;
+  d[25] = 0.0f;
   float R = 0.0f;
 #pragma unroll
-  for (int k = 0; k < 25; ++k) R = fmaxf(R, fabsf(w[k] - c));
+  for (int k = 0; k < 25; ++k) R = fmaxf(R, fabsf(d[k]));
   const bool flat = R <= kFlat * (fabsf(c) + 1e-12f);
   const float inv = flat ? 0.0f : 1.0f / R;
+#pragma unroll
+  for (int k = 0; k < 26; k += 2) {
+    const float2 q = __fmul2_rn(make_float2(d[k], d[k + 1]), make_float2(inv, inv));
+    d[k] = q.x;
+    d[k + 1] = q.y;
+  }
   auto val = [&](int k) -> float {
-    if (k < 25) return flat ? 0.0f : (w[k] - c) * inv;
+    if (k < 25) return d[k];
     return k == 25 ? tail0 : (k == 26 ? tail1 : 0.0f);
   };
 #pragma unroll

@@ -37,14 +37,43 @@ struct StageSmem32 {
 
 __device__ __forceinline__ float4 f4_split_store(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
 
-// Pointwise Lax-Friedrichs split of one node (flux_split in physics.cuh).
+// Packed FP32 pairs: Blackwell issues two FP32 adds, multiplies or FMAs of a
+// float2 as one instruction (round-to-nearest each, as the scalar forms), so
+// the per-component chains below run on the (x, y) and (z, w) halves of a
+// node's float4.
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 join2(const float2 a, const float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+// a - b, exactly as the scalar subtraction rounds it
+__device__ __forceinline__ float2 sub2(const float2 a, const float2 b) { return __ffma2_rn(b, splat2(-1.0f), a); }
+
+// Pointwise Lax-Friedrichs split of one node (flux_split in physics.cuh; the
+// same operations, F -+ ws U and the halving on packed pairs).
 template <int DIR>
 __device__ __forceinline__ void split4(float gamma, const float4 q, float4 &fm, float4 &fp) {
   const float U[4] = {q.x, q.y, q.z, q.w};
-  float m[4], p[4];
-  flux_split<float, DIR>(gamma, U, m, p);
-  fm = make_float4(m[0], m[1], m[2], m[3]);
-  fp = make_float4(p[0], p[1], p[2], p[3]);
+  float u, v, p;
+  primitives(gamma, U, u, v, p);
+  const float rho = q.x, E = q.w;
+  float F[4];
+  if (DIR == 0) {
+    F[0] = rho * u;
+    F[1] = rho * u * u + p;
+    F[2] = rho * u * v;
+    F[3] = (E + p) * u;
+  } else {
+    F[0] = rho * v;
+    F[1] = rho * u * v;
+    F[2] = rho * v * v + p;
+    F[3] = (E + p) * v;
+  }
+  const float c = tsqrt(tdiv(gamma * p, rho));
+  const float ws = (DIR == 0 ? tabs(u) : tabs(v)) + c;
+  const float2 h = splat2(0.5f), mws = splat2(-ws), pws = splat2(ws);
+  const float2 F01 = make_float2(F[0], F[1]), F23 = make_float2(F[2], F[3]);
+  fm = join2(__fmul2_rn(h, __ffma2_rn(mws, lo2(q), F01)), __fmul2_rn(h, __ffma2_rn(mws, hi2(q), F23)));
+  fp = join2(__fmul2_rn(h, __ffma2_rn(pws, lo2(q), F01)), __fmul2_rn(h, __ffma2_rn(pws, hi2(q), F23)));
 }
 
 // Linear fifth-order upwind flux of one component: WENO with its weights
@@ -60,13 +89,29 @@ __device__ __forceinline__ float lin5(float p0, float p1, float p2, float p3, fl
   return plus + minus;
 }
 
+// lin5 on two components at once (the same operation order).
+__device__ __forceinline__ float2 lin5x2(float2 p0, float2 p1, float2 p2, float2 p3, float2 p4, float2 m0, float2 m1,
+                                         float2 m2, float2 m3, float2 m4) {
+  const float2 c0 = splat2(float(2.0 / 60.0)), c1 = splat2(float(-13.0 / 60.0)), c2 = splat2(float(47.0 / 60.0)),
+               c3 = splat2(float(27.0 / 60.0)), c4 = splat2(float(-3.0 / 60.0));
+  float2 plus = __fmul2_rn(c0, p0);
+  plus = __ffma2_rn(c1, p1, plus);
+  plus = __ffma2_rn(c2, p2, plus);
+  plus = __ffma2_rn(c3, p3, plus);
+  plus = __ffma2_rn(c4, p4, plus);
+  float2 minus = __fmul2_rn(c0, m4);
+  minus = __ffma2_rn(c1, m3, minus);
+  minus = __ffma2_rn(c2, m2, minus);
+  minus = __ffma2_rn(c3, m1, minus);
+  minus = __ffma2_rn(c4, m0, minus);
+  return __fadd2_rn(plus, minus);
+}
+
 __device__ __forceinline__ float4 linear_face4(const float4 *P, const float4 *M, int ss) {
   const float4 p0 = P[0], p1 = P[ss], p2 = P[2 * ss], p3 = P[3 * ss], p4 = P[4 * ss];
   const float4 m0 = M[0], m1 = M[ss], m2 = M[2 * ss], m3 = M[3 * ss], m4 = M[4 * ss];
-  return make_float4(lin5(p0.x, p1.x, p2.x, p3.x, p4.x, m0.x, m1.x, m2.x, m3.x, m4.x),
-                     lin5(p0.y, p1.y, p2.y, p3.y, p4.y, m0.y, m1.y, m2.y, m3.y, m4.y),
-                     lin5(p0.z, p1.z, p2.z, p3.z, p4.z, m0.z, m1.z, m2.z, m3.z, m4.z),
-                     lin5(p0.w, p1.w, p2.w, p3.w, p4.w, m0.w, m1.w, m2.w, m3.w, m4.w));
+  return join2(lin5x2(lo2(p0), lo2(p1), lo2(p2), lo2(p3), lo2(p4), lo2(m0), lo2(m1), lo2(m2), lo2(m3), lo2(m4)),
+               lin5x2(hi2(p0), hi2(p1), hi2(p2), hi2(p3), hi2(p4), hi2(m0), hi2(m1), hi2(m2), hi2(m3), hi2(m4)));
 }
 
 // Characteristic WENO face from float4 stencils (face_flux_st).
@@ -330,7 +375,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     const int t = threadIdx.x + k * NT;
     if (t < TI * TJ) {
       const float4 hr = Hf[t + TJ], hl = Hf[t];
-      rhs[k] = make_float4(-(hr.x - hl.x) * idx, -(hr.y - hl.y) * idx, -(hr.z - hl.z) * idx, -(hr.w - hl.w) * idx);
+      const float2 mi = splat2(-idx);  // -(hr - hl) * idx, the negation exact
+      rhs[k] = join2(__fmul2_rn(sub2(lo2(hr), lo2(hl)), mi), __fmul2_rn(sub2(hi2(hr), hi2(hl)), mi));
     }
   }
   if constexpr (ROUTE) {
@@ -394,8 +440,10 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     const int i = t / TJ, j = t - (t / TJ) * TJ;
     if (i0 + i >= g.nx || j0 + j >= g.ny) continue;
     const float4 hr = Hf[i * (TJ + 1) + j + 1], hl = Hf[i * (TJ + 1) + j];
-    float rr[4] = {rhs[k].x - (hr.x - hl.x) * idy, rhs[k].y - (hr.y - hl.y) * idy, rhs[k].z - (hr.z - hl.z) * idy,
-                   rhs[k].w - (hr.w - hl.w) * idy};
+    const float2 mi = splat2(-idy);  // rhs - (hr - hl) * idy
+    const float2 r01 = __ffma2_rn(sub2(lo2(hr), lo2(hl)), mi, lo2(rhs[k]));
+    const float2 r23 = __ffma2_rn(sub2(hi2(hr), hi2(hl)), mi, hi2(rhs[k]));
+    float rr[4] = {r01.x, r01.y, r23.x, r23.y};
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
       const float4 q = Us[(i + 3) * HJ + j + 3];
       rr[3] += q.z * 1.0f;
