@@ -65,6 +65,17 @@ __device__ __forceinline__ void flux_split(T gamma, const T U[4], T fm[4], T fp[
   }
 }
 
+// Packed FP32 pairs: Blackwell issues two FP32 adds, multiplies or FMAs of a
+// float2 as one instruction (round-to-nearest each, as the scalar forms), so
+// the per-component chains below run on the (x, y) and (z, w) halves of a
+// node's float4.
+__device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 join2(const float2 a, const float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+// a - b, exactly as the scalar subtraction rounds it
+__device__ __forceinline__ float2 sub2(const float2 a, const float2 b) { return __ffma2_rn(b, splat2(-1.0f), a); }
+
 // ---------------------------------------------------------------- WENO
 
 // Smoothness indicators shared by all four schemes (include/Utility.hpp
@@ -211,6 +222,79 @@ __device__ __forceinline__ T weno(T a, T b, T c, T d, T e, T zp_lambda) {
   return weno_zpi(a, b, c, d, e);
 }
 
+// WENO-JS / WENO-Z on two stencils at once (betas, wenoz_weights or the
+// WENO-JS weights, and combine of physics.cuh, in the same order), used for
+// the + and - sides of one characteristic field: the arithmetic runs on packed
+// pairs, the reciprocals and the caps per element.
+__device__ __forceinline__ void betas2(float2 a, float2 b, float2 c, float2 d, float2 e, float2 &bm, float2 &b0,
+                                       float2 &bp) {
+  const float2 c1312 = splat2(float(13.0 / 12.0)), c14 = splat2(0.25f), m2 = splat2(-2.0f), m4 = splat2(-4.0f),
+               p3 = splat2(3.0f);
+  float2 t1 = __fadd2_rn(__ffma2_rn(m2, b, a), c);
+  float2 t2 = __ffma2_rn(p3, c, __ffma2_rn(m4, b, a));
+  bm = __ffma2_rn(__fmul2_rn(c1312, t1), t1, __fmul2_rn(__fmul2_rn(c14, t2), t2));
+  t1 = __fadd2_rn(__ffma2_rn(m2, c, b), d);
+  t2 = sub2(b, d);
+  b0 = __ffma2_rn(__fmul2_rn(c1312, t1), t1, __fmul2_rn(__fmul2_rn(c14, t2), t2));
+  t1 = __fadd2_rn(__ffma2_rn(m2, d, c), e);
+  t2 = __fadd2_rn(__ffma2_rn(m4, d, __fmul2_rn(p3, c)), e);
+  bp = __ffma2_rn(__fmul2_rn(c1312, t1), t1, __fmul2_rn(__fmul2_rn(c14, t2), t2));
+}
+
+__device__ __forceinline__ float2 rcp2(float2 x) { return make_float2(__fdividef(1.0f, x.x), __fdividef(1.0f, x.y)); }
+
+template <int SCHEME>
+__device__ __forceinline__ float2 weno2(float2 a, float2 b, float2 c, float2 d, float2 e) {
+  static_assert(SCHEME == kWenoJS || SCHEME == kWenoZ, "packed WENO-JS and WENO-Z only");
+  float2 bm, b0, bp, w0, w1, w2;
+  betas2(a, b, c, d, e, bm, b0, bp);
+  if constexpr (SCHEME == kWenoZ) {
+    const float2 eps = splat2(1.0e-20f), one = splat2(1.0f);
+    const float2 ibm = rcp2(__fadd2_rn(bm, eps)), ib0 = rcp2(__fadd2_rn(b0, eps)), ibp = rcp2(__fadd2_rn(bp, eps));
+    const float2 tau = make_float2(fabsf(bm.x - bp.x), fabsf(bm.y - bp.y));
+    float2 rm = __fmul2_rn(tau, ibm), r0 = __fmul2_rn(tau, ib0), rp = __fmul2_rn(tau, ibp);
+    rm = make_float2(fminf(rm.x, 1.0e18f), fminf(rm.y, 1.0e18f));
+    r0 = make_float2(fminf(r0.x, 1.0e18f), fminf(r0.y, 1.0e18f));
+    rp = make_float2(fminf(rp.x, 1.0e18f), fminf(rp.y, 1.0e18f));
+    w0 = __fmul2_rn(splat2(0.1f), __ffma2_rn(rm, rm, one));
+    w1 = __fmul2_rn(splat2(0.6f), __ffma2_rn(r0, r0, one));
+    w2 = __fmul2_rn(splat2(0.3f), __ffma2_rn(rp, rp, one));
+  } else {
+    const float2 eps = splat2(1.0e-6f);
+    const float2 sm = __fadd2_rn(eps, bm), s0 = __fadd2_rn(eps, b0), sp = __fadd2_rn(eps, bp);
+    w0 = __fmul2_rn(splat2(0.1f), rcp2(__fmul2_rn(sm, sm)));
+    w1 = __fmul2_rn(splat2(0.6f), rcp2(__fmul2_rn(s0, s0)));
+    w2 = __fmul2_rn(splat2(0.3f), rcp2(__fmul2_rn(sp, sp)));
+  }
+  const float2 iws = rcp2(__fadd2_rn(__fadd2_rn(w0, w1), w2));
+  w0 = __fmul2_rn(w0, iws);
+  w1 = __fmul2_rn(w1, iws);
+  w2 = __fmul2_rn(w2, iws);
+  const float2 c13 = splat2(float(1.0 / 3.0)), c56 = splat2(float(5.0 / 6.0)), c116 = splat2(float(11.0 / 6.0));
+  const float2 mc76 = splat2(-float(7.0 / 6.0)), mc16 = splat2(-float(1.0 / 6.0));
+  const float2 q0 = __ffma2_rn(c116, c, __ffma2_rn(mc76, b, __fmul2_rn(c13, a)));
+  const float2 q1 = __ffma2_rn(c13, d, __ffma2_rn(c56, c, __fmul2_rn(mc16, b)));
+  const float2 q2 = __ffma2_rn(mc16, e, __ffma2_rn(c56, d, __fmul2_rn(c13, c)));
+  return __ffma2_rn(w2, q2, __ffma2_rn(w1, q1, __fmul2_rn(w0, q0)));
+}
+
+// The two sides of one characteristic field at a face: the + side on F+
+// stencil values p0..p4, the - side on F- values mirrored (m4..m0), summed.
+// FP64 evaluates them one after the other as the reference does; FP32
+// WENO-JS and WENO-Z evaluate both at once on packed pairs.
+template <typename T, int SCHEME>
+__device__ __forceinline__ T weno_sides(const T vp[5], const T vm[5], T zp_lambda) {
+  if constexpr (sizeof(T) == 4 && (SCHEME == kWenoJS || SCHEME == kWenoZ)) {
+    const float2 r = weno2<SCHEME>(make_float2(vp[0], vm[4]), make_float2(vp[1], vm[3]), make_float2(vp[2], vm[2]),
+                                   make_float2(vp[3], vm[1]), make_float2(vp[4], vm[0]));
+    return r.x + r.y;
+  } else {
+    const T hp = weno<T, SCHEME>(vp[0], vp[1], vp[2], vp[3], vp[4], zp_lambda);
+    const T hm = weno<T, SCHEME>(vm[4], vm[3], vm[2], vm[1], vm[0], zp_lambda);
+    return hp + hm;
+  }
+}
+
 // ------------------------------------------------------- one face flux
 
 // Characteristic WENO flux at one face (src/WENOFD.cpp:526-643 in x,
@@ -297,9 +381,7 @@ __device__ __forceinline__ void face_flux_st(T gamma, T zp_lambda, const T um[4]
       y += l3 * fm(s, 3);
       vm[s] = y;
     }
-    const T hp = weno<T, SCHEME>(vp[0], vp[1], vp[2], vp[3], vp[4], zp_lambda);
-    const T hm = weno<T, SCHEME>(vm[4], vm[3], vm[2], vm[1], vm[0], zp_lambda);
-    vh[k] = hp + hm;
+    vh[k] = weno_sides<T, SCHEME>(vp, vm, zp_lambda);
   }
 
   // R * vh, rows in the reference's order (utils/equations.hpp:239-299).
