@@ -49,6 +49,10 @@ SEED = 2024
 THRESHOLD = 0.8
 LABEL_DEVIATION = 1e-2
 INDICATOR_INTERVAL = 3  # time steps per indicator run (--indicator-interval)
+# Training is repeatable bit for bit; of training seeds 1-8 this one gave the
+# lowest binary cross-entropy on held-out stencils (solver runs at seeds used
+# neither for training nor for the workload).
+TRAIN_SEED = 7
 METRIC = "cell-updates/s at 4096^2 (learned+FP32 vs plain FP64 WENO-Z, same GB300) at stated L1 err"
 # algorithmic HBM bytes per node for one SSP-RK3 step with FP64 state:
 # stage 1 reads U^n, writes U1 (64 B); stages 2, 3 read U^n and U^k, write (96 B each)
@@ -242,10 +246,10 @@ def train_indicator(torch, device: int):
     t0 = time.perf_counter()
     X, y = learned.generate_dataset(torch, device=device, label_deviation=LABEL_DEVIATION)
     t1 = time.perf_counter()
-    params, losses = learned.train(torch, X, y, epochs=30, batch=4096, lr=3e-3)
+    params, losses = learned.train(torch, X, y, epochs=30, batch=4096, lr=3e-3, seed=TRAIN_SEED)
     t2 = time.perf_counter()
     recall, precision, _ = learned.recall_precision(torch, params, X[:200000], y[:200000], THRESHOLD)
-    info = {"samples": int(len(y)), "positive_fraction": float(y.mean()), "epochs": 30,
+    info = {"samples": int(len(y)), "positive_fraction": float(y.mean()), "epochs": 30, "seed": TRAIN_SEED,
             "loss_first_epoch": float(losses[0]), "loss_last_epoch": float(losses[-1]),
             "recall": recall, "precision": precision, "threshold": THRESHOLD, "label_deviation": LABEL_DEVIATION,
             "indicator_interval": INDICATOR_INTERVAL,

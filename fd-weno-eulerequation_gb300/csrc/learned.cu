@@ -47,11 +47,12 @@ __global__ void k_mlp_forward(const float *P, const float *X, long long n, float
 // One block = kBB samples of the batch.  Per sample: forward, dL/dlogit of
 // the mean binary cross-entropy (scaled by inv_n), back-propagation to dz1,
 // dz2.  Then the block sums the weight gradients over its samples and adds
-// them (and its loss share) to grad / loss with one atomic per entry.
+// them (and its loss share) to grad / loss with one atomic per entry, or,
+// given `part`, writes them to its own row there for an ordered sum.
 constexpr int kBB = 128;
 
 __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const float *X, const float *Y, long long n,
-                                                      float inv_n, float *grad, float *loss) {
+                                                      float inv_n, float *grad, float *loss, float *part) {
   extern __shared__ float sm[];
   float *sp = sm;                  // kParams
   float *sx = sp + kParams;        // kBB * kIn
@@ -117,13 +118,27 @@ __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const floa
     } else {
       for (int s = 0; s < kBB; ++s) acc += sd[s];
     }
-    atomicAdd(&grad[e], acc);
+    if (part) part[(long long)blockIdx.x * (kParams + 1) + e] = acc;
+    else atomicAdd(&grad[e], acc);
   }
   if (threadIdx.x == 0) {
     float l = 0.0f;
     for (int s = 0; s < kBB; ++s) l += sl[s];
-    atomicAdd(loss, l);
+    if (part) part[(long long)blockIdx.x * (kParams + 1) + kParams] = l;
+    else atomicAdd(loss, l);
   }
+}
+
+// The blocks' partial gradients (and loss shares) summed in block order:
+// the training loop's gradient does not depend on the order in which the
+// blocks finished, so a training run is repeatable bit for bit.
+__global__ void k_grad_reduce(const float *part, int blocks, float *grad, float *loss) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e > kParams) return;
+  float acc = 0.0f;
+  for (int b = 0; b < blocks; ++b) acc += part[(long long)b * (kParams + 1) + e];
+  if (e < kParams) grad[e] = acc;
+  else *loss = acc;
 }
 
 __global__ void k_adam(float *P, const float *G, float *M, float *V, int step, float lr) {
@@ -584,24 +599,40 @@ extern "C" int wenofd_mlp_forward(const float *dev_params, const float *dev_x, l
   return cudaGetLastError() == cudaSuccess ? WENOFD_OK : WENOFD_CUDA_ERROR;
 }
 
-extern "C" int wenofd_mlp_backward(const float *dev_params, const float *dev_x, const float *dev_y, long long n,
-                                   float *dev_grad, float *dev_loss, void *stream) {
+namespace {
+
+// One backward pass over n samples: with part null the blocks add their
+// gradients into grad / loss with atomics (after zeroing them); with part
+// (room for one row of kParams + 1 floats per block) they write partials and
+// k_grad_reduce sums them in block order.
+int launch_backward(const float *params, const float *x, const float *y, long long n, float *grad, float *loss,
+                    float *part, cudaStream_t s) {
   using namespace wenofd::lrn;
-  if (!dev_params || !dev_x || !dev_y || !dev_grad || !dev_loss || n <= 0) return WENOFD_BAD_ARG;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t smem = sizeof(float) * (kParams + kBB * kIn + 4 * kBB * kHid + 2 * kBB);
-  static bool configured = false;
-  if (!configured) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return WENOFD_CUDA_ERROR;
+  static unsigned long long configured = 0;  // one bit per device
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(configured & bit)) {
     if (cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)) != cudaSuccess)
       return WENOFD_CUDA_ERROR;
-    configured = true;
+    configured |= bit;
   }
-  if (cudaMemsetAsync(dev_grad, 0, kParams * sizeof(float), s) != cudaSuccess ||
-      cudaMemsetAsync(dev_loss, 0, sizeof(float), s) != cudaSuccess)
-    return WENOFD_CUDA_ERROR;
   const long long blocks = (n + kBB - 1) / kBB;
-  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(dev_params, dev_x, dev_y, n, 1.0f / float(n), dev_grad, dev_loss);
+  if (!part && (cudaMemsetAsync(grad, 0, kParams * sizeof(float), s) != cudaSuccess ||
+                cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess))
+    return WENOFD_CUDA_ERROR;
+  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(params, x, y, n, 1.0f / float(n), grad, loss, part);
+  if (part) k_grad_reduce<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(part, int(blocks), grad, loss);
   return cudaGetLastError() == cudaSuccess ? WENOFD_OK : WENOFD_CUDA_ERROR;
+}
+
+}  // namespace
+
+extern "C" int wenofd_mlp_backward(const float *dev_params, const float *dev_x, const float *dev_y, long long n,
+                                   float *dev_grad, float *dev_loss, void *stream) {
+  if (!dev_params || !dev_x || !dev_y || !dev_grad || !dev_loss || n <= 0) return WENOFD_BAD_ARG;
+  return launch_backward(dev_params, dev_x, dev_y, n, dev_grad, dev_loss, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *dev_m, float *dev_v, int step,
@@ -614,15 +645,21 @@ extern "C" int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *
 
 // Training loop: per epoch a seeded shuffle of the mini-batch order, and per
 // mini-batch one backward pass and one Adam step.  The epoch's mean loss is
-// read back once per epoch.
+// read back once per epoch.  Each mini-batch's gradient is summed in block
+// order (k_grad_reduce), so the same data and seed give the same parameters
+// bit for bit.
 extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs,
                                 int batch, float lr, unsigned long long seed, float *host_epoch_loss, void *stream) {
   using namespace wenofd::lrn;
   if (!dev_params || !dev_x || !dev_y || n <= 0 || epochs < 1 || batch < 1) return WENOFD_BAD_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  float *buf = nullptr;  // grad | m | v | loss | epoch loss
-  if (cudaMalloc(&buf, sizeof(float) * (3 * kParams + 2)) != cudaSuccess) return WENOFD_CUDA_ERROR;
+  // grad | m | v | loss | epoch loss | the backward blocks' partial rows
+  const long long part_rows = (std::min<long long>(batch, n) + kBB - 1) / kBB;
+  float *buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(float) * (3 * kParams + 2 + part_rows * (kParams + 1))) != cudaSuccess)
+    return WENOFD_CUDA_ERROR;
   float *grad = buf, *m = buf + kParams, *v = buf + 2 * kParams, *loss = buf + 3 * kParams;
+  float *part = buf + 3 * kParams + 2;
   int rc = WENOFD_OK;
   if (cudaMemsetAsync(m, 0, sizeof(float) * 2 * kParams, s) != cudaSuccess) rc = WENOFD_CUDA_ERROR;
   const long long nb = (n + batch - 1) / batch;
@@ -644,7 +681,7 @@ extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const flo
     for (long long k = 0; k < nb && rc == WENOFD_OK; ++k) {
       const long long off = order[k] * batch;
       const long long cnt = off + batch <= n ? batch : n - off;
-      rc = wenofd_mlp_backward(dev_params, dev_x + off * kIn, dev_y + off, cnt, grad, loss, stream);
+      rc = launch_backward(dev_params, dev_x + off * kIn, dev_y + off, cnt, grad, loss, part, s);
       if (rc == WENOFD_OK) rc = wenofd_mlp_adam(dev_params, grad, m, v, ++step, lr, stream);
       if (rc == WENOFD_OK && host_epoch_loss && (k == nb - 1 || k % 16 == 0)) {
         float l = 0.0f;

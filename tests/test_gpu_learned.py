@@ -149,6 +149,19 @@ def test_trained_indicator_gain_over_the_method_without_it():
           f"FP32 WENO {e_weno:.3e}; recall {recall:.3f} precision {precision:.3f}")
 
 
+def test_training_is_repeatable():
+    """The training loop sums each mini-batch's gradient in block order, so
+    the same stencils and seed give the same parameters bit for bit (and so
+    the same flags in the time loop)."""
+    X, y = learned.generate_dataset(torch, runs=((5, 41),), n=128, snapshots=(10, 30), per_snapshot=12_000)
+    a, la = learned.train(torch, X, y, epochs=3, batch=1024, lr=3e-3, seed=5)
+    b, lb = learned.train(torch, X, y, epochs=3, batch=1024, lr=3e-3, seed=5)
+    assert np.array_equal(a, b)
+    assert np.array_equal(np.asarray(la), np.asarray(lb))
+    c, _ = learned.train(torch, X, y, epochs=3, batch=1024, lr=3e-3, seed=6)
+    assert not np.array_equal(a, c)  # the seed does reach the mini-batch order
+
+
 def test_learned_error_against_finer_reference_within_bound():
     """The accuracy bar of the learned + FP32 form: its L1 density error
     against a 2x finer plain FP64 WENO-Z solution (node-based refinement,
