@@ -66,9 +66,10 @@ __device__ __forceinline__ void flux_split(T gamma, const T U[4], T fm[4], T fp[
 }
 
 // Packed FP32 pairs: Blackwell issues two FP32 adds, multiplies or FMAs of a
-// float2 as one instruction (round-to-nearest each, as the scalar forms), so
-// the per-component chains below run on the (x, y) and (z, w) halves of a
-// node's float4.
+// float2 as one instruction (round-to-nearest each, as the scalar forms).
+// The FP32 forms run independent chains on pairs: the (x, y) and (z, w)
+// halves of a node's float4 (stage_f32.cuh), and the two sides of a
+// characteristic field's reconstruction (weno2 below).
 __device__ __forceinline__ float2 lo2(const float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(const float4 v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float4 join2(const float2 a, const float2 b) { return make_float4(a.x, a.y, b.x, b.y); }

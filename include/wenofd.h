@@ -186,7 +186,10 @@ int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *
  *             its gradient into grad[WENOFD_MLP_PARAMS] (both overwritten);
  *   adam: one Adam step (beta 0.9 / 0.999, eps 1e-8), step counts from 1;
  *   train: epochs of shuffled mini-batches of backward + adam, the mean loss
- *          of each epoch to host_epoch_loss[epochs] (may be NULL). */
+ *          of each epoch to host_epoch_loss[epochs] (may be NULL); each
+ *          mini-batch's gradient is summed in a fixed order, so the same
+ *          data and seed give the same parameters bit for bit (the
+ *          standalone backward accumulates with atomics). */
 int wenofd_mlp_forward(const float *dev_params, const float *dev_x, long long n, float *dev_logits, void *stream);
 int wenofd_mlp_backward(const float *dev_params, const float *dev_x, const float *dev_y, long long n,
                         float *dev_grad, float *dev_loss, void *stream);
