@@ -157,7 +157,25 @@ def cpu_baseline(budget_s: float = 12.0) -> dict:
             break
     return {"value": steps * N * N / el, "unit": "cell-updates/s", "cores": threads, "kind": "port",
             "sample": f"{steps} RK3 step(s) of the 4096^2 shear layer, oracle C restatement, "
-                      f"{threads} OpenMP threads, {el:.1f} s"}
+                      f"{threads} OpenMP threads, {el:.1f} s",
+            "single_core": cpu_single_core()}
+
+
+def cpu_single_core(n: int = 1024) -> dict | None:
+    """The same restatement on one thread (a separate process, so that its
+    OpenMP runtime starts with one thread): one RK3 step of the shear layer
+    at n^2."""
+    code = ("import time, oracle as orc\n"
+            f"p = orc.Problem(orc.SHEAR, {n}, {n}, orc.WENOZ, 2, 0.7, seed={SEED}, t_end=1e9)\n"
+            "dt = p.calc_dt()\nt0 = time.perf_counter()\np.rk_step(dt)\nprint(time.perf_counter() - t0)\n")
+    env = dict(os.environ, OMP_NUM_THREADS="1", PYTHONPATH=os.path.join(ROOT, "oracle"))
+    try:
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        el = float(r.stdout.strip().splitlines()[-1])
+    except (subprocess.SubprocessError, ValueError, IndexError):
+        return None
+    return {"value": n * n / el, "unit": "cell-updates/s", "cores": 1,
+            "sample": f"1 RK3 step of the {n}^2 shear layer, oracle C restatement, 1 thread, {el:.1f} s"}
 
 
 def run_reference_arm(args) -> None:

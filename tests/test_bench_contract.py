@@ -35,6 +35,8 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert isinstance(cb["sample"], str) and cb["sample"]
+    one = cb["single_core"]
+    assert one["cores"] == 1 and one["value"] > 0 and one["unit"] == d["unit"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 
