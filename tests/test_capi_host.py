@@ -39,6 +39,12 @@ def test_version_string():
     ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": -1.0, "SCHEME": 1}, "CFL"),
     ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "PRECISION": 4},
      "PRECISION"),
+    ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "INDICATOR_INTERVAL": 0},
+     "INDICATOR_INTERVAL"),
+    ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "LABEL_DEVIATION": 0},
+     "LABEL_DEVIATION"),
+    ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1,
+      "LABEL_DEVIATION": "x"}, "LABEL_DEVIATION"),
 ])
 def test_bad_config_is_rejected(cfg, needle):
     with pytest.raises(wenofd.WenofdError) as e:
