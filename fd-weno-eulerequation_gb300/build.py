@@ -69,6 +69,15 @@ def _run(cmd: list[str]) -> str:
     return r.stdout + r.stderr
 
 
+def build_pipe_peaks() -> str:
+    """Opt-in measurement tool (not part of the library): FP64/FP32 pipe and
+    host-link peaks, fd-weno-eulerequation_gb300/_build/pipe_peaks."""
+    os.makedirs(OUT, exist_ok=True)
+    probe = os.path.join(OUT, "pipe_peaks")
+    _run([NVCC] + ARCH + ["-O3", "-std=c++17", os.path.join(PKG, "tools", "pipe_peaks.cu"), "-o", probe])
+    return probe
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     jobs = []
@@ -96,10 +105,6 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if jobs or not os.path.exists(LIB):
         lib_dir = os.path.join(CUDA_HOME, "lib64")
         _run([NVCC] + ARCH + ["-shared", "-cudart", "shared", "-Xlinker", "-rpath," + lib_dir] + objs + ["-o", LIB])
-    probe = os.path.join(OUT, "pipe_peaks")
-    probe_src = os.path.join(CSRC, "pipe_peaks.cu")
-    if force or not os.path.exists(probe) or os.path.getmtime(probe_src) > os.path.getmtime(probe):
-        _run([NVCC] + ARCH + ["-O3", "-std=c++17", probe_src, "-o", probe])
     host_srcs = [os.path.join(HOST, f) for f in ("WENOFD.cpp", "main.cpp")]
     if all(os.path.exists(p) for p in host_srcs) and (force or not os.path.exists(EXE) or any(
             os.path.getmtime(p) > os.path.getmtime(EXE) for p in host_srcs + [LIB, os.path.join(HOST, "WENOFD.hpp")])):
@@ -112,7 +117,10 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--force", action="store_true")
     ap.add_argument("--verbose-ptxas", action="store_true")
+    ap.add_argument("--pipe-peaks", action="store_true", help="also build the pipe/link peak measurement tool")
     a = ap.parse_args()
+    if a.pipe_peaks:
+        print(build_pipe_peaks())
     out = build(a.force, a.verbose_ptxas)
     if out.strip():
         sys.stdout.write(out)

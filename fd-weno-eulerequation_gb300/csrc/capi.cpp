@@ -221,6 +221,7 @@ void release(wenofd_solver *s) {
   if (!s) return;
   cudaSetDevice(s->device);
   if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph1) cudaGraphExecDestroy(s->graph1);
   cudaFree(s->S);
   cudaFree(s->A);
   cudaFree(s->B);
@@ -586,6 +587,47 @@ int wenofd_step(wenofd_solver *s, double *dt_out) {
   return WENOFD_OK;
 }
 
+namespace {
+
+// Captures `nsteps` graph-driven steps into an executable graph on a private
+// stream; *kernels receives the kernel nodes it holds.
+int capture_steps(wenofd_solver *s, int nsteps, cudaGraphExec_t *exec, long long *kernels) {
+  cudaStream_t cap = nullptr;
+  CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaStream_t keep = s->stream;
+  s->stream = cap;
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  int rc = WENOFD_OK;
+  const long long before = s->launches;
+  if (ce == cudaSuccess) {
+    for (int k = 0; k < nsteps && rc == WENOFD_OK; ++k) rc = enqueue_step(s);
+    ce = cudaStreamEndCapture(cap, &graph);
+  }
+  *kernels = s->launches - before;
+  s->launches = before;
+  s->stream = keep;
+  cudaStreamDestroy(cap);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  CUDA_TRY(ce);
+  ce = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CUDA_TRY(ce);
+  return WENOFD_OK;
+}
+
+void drop_graphs(wenofd_solver *s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph1) cudaGraphExecDestroy(s->graph1);
+  s->graph = nullptr;
+  s->graph1 = nullptr;
+}
+
+}  // namespace
+
 int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done) {
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
@@ -602,31 +644,27 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
     // small grids, one step on large ones.
     const long long cells = (long long)s->nx * s->ny;
     s->graph_steps = int(std::max(1LL, std::min(64LL, (4LL << 20) / std::max(1LL, cells))));
-    cudaStream_t cap = nullptr;
-    CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-    cudaStream_t keep = s->stream;
-    s->stream = cap;
-    cudaGraph_t graph = nullptr;
-    CUDA_TRY(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-    int rc = WENOFD_OK;
-    const long long before = s->launches;
-    for (int k = 0; k < s->graph_steps && rc == WENOFD_OK; ++k) rc = enqueue_step(s);
-    s->graph_kernels = s->launches - before;
-    s->launches = before;
-    cudaError_t ce = cudaStreamEndCapture(cap, &graph);
-    s->stream = keep;
-    cudaStreamDestroy(cap);
-    if (rc) return rc;
-    CUDA_TRY(ce);
-    ce = cudaGraphInstantiate(&s->graph, graph, 0);
-    cudaGraphDestroy(graph);
-    CUDA_TRY(ce);
+    if (int rc = capture_steps(s, s->graph_steps, &s->graph, &s->graph_kernels)) return rc;
   }
   CUDA_TRY(wenofd::launch_advance_setup(s->ctrl, max_steps, s->stream));
   s->launches += 1;
+  // Steps this call may still take (-1: no cap).  A chunk past the cap runs
+  // gated-off launches that return at once; when fewer steps than a chunk
+  // remain, one-step graphs are replayed instead.
+  long long left = max_steps < 0 ? -1 : max_steps;
   for (;;) {
-    CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
-    s->launches += s->graph_kernels;
+    if (left >= 0 && left < s->graph_steps) {
+      if (!s->graph1) {
+        if (int rc = capture_steps(s, 1, &s->graph1, &s->graph1_kernels)) return rc;
+      }
+      for (long long k = 0; k < left; ++k) {
+        CUDA_TRY(cudaGraphLaunch(s->graph1, s->stream));
+        s->launches += s->graph1_kernels;
+      }
+    } else {
+      CUDA_TRY(cudaGraphLaunch(s->graph, s->stream));
+      s->launches += s->graph_kernels;
+    }
     if (int rc = read_ctrl(s)) return rc;
     const Ctrl &c = *s->ctrl_host;
     if (s->ind_error) {
@@ -639,6 +677,7 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
       return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
     }
     if (c.done || c.steps >= c.max_steps) break;
+    if (left >= 0) left = c.max_steps - c.steps;
   }
   if (steps_done) *steps_done = s->ctrl_host->steps - start;
   return WENOFD_OK;
@@ -707,10 +746,9 @@ int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float thres
   s->ind_logit_threshold = std::log(threshold / (1.0f - threshold));
   if (int rc = sync(s)) return rc;
   s->ind_ready = true;
-  // the time-loop graph holds the indicator launch and its threshold: capture
-  // it again on the next advance
-  if (s->graph) cudaGraphExecDestroy(s->graph);
-  s->graph = nullptr;
+  // the time-loop graphs hold the indicator launch and its threshold: capture
+  // them again on the next advance
+  drop_graphs(s);
   return WENOFD_OK;
 }
 

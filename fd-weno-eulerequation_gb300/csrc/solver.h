@@ -34,9 +34,11 @@ struct wenofd_solver {
   double label_deviation = 1e-2;  // LABEL_DEVIATION: training-label threshold
   int ind_interval = 1;            // INDICATOR_INTERVAL: steps per indicator run in the time loop
   bool ind_ready = false;
-  cudaGraphExec_t graph = nullptr;
+  cudaGraphExec_t graph = nullptr;   // graph_steps steps of the time loop
+  cudaGraphExec_t graph1 = nullptr;  // one step, for the tail of a capped advance
   int graph_steps = 0;
-  long long graph_kernels = 0;  // kernel nodes in the graph
+  long long graph_kernels = 0;   // kernel nodes in the graph
+  long long graph1_kernels = 0;  // kernel nodes in graph1
   long long launches = 0;       // kernels enqueued so far (graph replays included)
 };
 

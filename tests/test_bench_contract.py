@@ -19,8 +19,8 @@ def _run(args, env_extra=None, timeout=300):
 
 
 def test_reference_arm_line():
-    # 20 + 4 steps keep the CPU sample at its 5 s floor
-    r = _run(["--impl", "reference", "--steps", "20", "--warmup", "4"])
+    # the line's format on a 256^2 grid (the default 4096^2 takes ~4 s per step here)
+    r = _run(["--impl", "reference", "--steps", "5", "--warmup", "3", "--grid", "256"])
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
     assert len(lines) == 1
@@ -30,8 +30,9 @@ def test_reference_arm_line():
               "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["unit"] == "cell-updates/s" and d["higher_is_better"] is True and d["value"] > 0
-    assert d["steps"] == 20 and d["warmup"] == 4
-    assert "workload" in d["config"]
+    assert d["steps"] == 5 and d["warmup"] == 3
+    assert d["config"]["workload"] == "shear layer 256x256, SSP-RK3, WENO-Z, CFL 0.7, seed 2024"
+    assert "5 timed" in d["cpu_baseline"]["sample"] and d["ms_per_step"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert isinstance(cb["sample"], str) and cb["sample"]

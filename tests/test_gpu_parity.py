@@ -4,7 +4,10 @@ FP64 with WENO-JS / WENO-Z must equal the reference bit for bit (compared
 with ==, so +0 and -0 agree): RHS, ghost fill, time step, and the state
 after N steps.  WENO-ZP / WENO-ZPI evaluate the reference's pow(x, 2) as the
 correctly rounded x*x while glibc's pow is off by one ulp on ~0.1% of inputs,
-so those two schemes are held to a 1e-12 relative bound instead.
+so those two schemes are held to a 1e-12 relative bound instead.  Whole runs
+at the drop-in configuration's sizes (800^2 to t = 0.3, 4096^2 for 20 steps)
+and against the reference built with its own flags are in
+test_gpu_parity_long.py.
 """
 import numpy as np
 import pytest
@@ -102,29 +105,6 @@ def test_odd_sizes_match_oracle(tc, scheme, rk):
         assert_same(s.get_state(), p.interior(), "state")
 
 
-def _riemann_full(n, steps, seed=7):
-    p = orc.Problem(orc.RIEMANN_SEEDED, n, n, orc.WENOZ, 2, 0.7, seed=seed, t_end=0.3)
-    init = p.interior()
-    with wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7,
-                        "SCHEME": 1, "SEED": seed}) as s:
-        s.set_state(init)
-        assert s.advance(max_steps=steps) == steps
-        gpu = s.get_state()
-    p.run(max_steps=steps)
-    return gpu, p.interior()
-
-
-def test_riemann_800_matches_oracle():
-    gpu, cpu = _riemann_full(800, 40)
-    assert_same(gpu, cpu, "800^2 after 40 RK3 steps")
-
-
-def test_riemann_4096_matches_oracle():
-    """Full-size configuration: 4096^2 seeded four-quadrant Riemann problem."""
-    gpu, cpu = _riemann_full(4096, 2)
-    assert_same(gpu, cpu, "4096^2 after 2 RK3 steps")
-
-
 def test_nan_state_reports_nan_dt():
     p = orc.Problem(orc.RIEMANN2, 16, 16)
     U = p.interior()
@@ -137,3 +117,21 @@ def test_nan_state_reports_nan_dt():
         with pytest.raises(wenofd.WenofdError) as e:
             s.advance(max_steps=3)
         assert e.value.status == wenofd.NAN_DT
+
+
+def test_short_advance_runs_only_its_steps():
+    """A capped advance shorter than a graph chunk replays one-step graphs, so
+    it launches the kernels of its own steps and no gated-off chunk tail."""
+    with wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": 48, "ELEMNUMY": 40, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
+                        "SEED": 2}) as s:
+        s.initialize()
+        assert s.advance(max_steps=1) == 1
+        per_step = 10  # gate, time step, finalize, 3 x (ghost fill, stage), time update
+        assert s.info().graph_steps == 64
+        l0 = s.info().launches
+        assert s.advance(max_steps=5) == 5
+        assert s.info().launches - l0 == 1 + 5 * per_step
+        l0 = s.info().launches
+        assert s.advance(max_steps=70) == 70
+        assert s.info().launches - l0 == 1 + 70 * per_step
+        assert s.info().steps == 76
