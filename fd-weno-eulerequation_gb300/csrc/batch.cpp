@@ -43,6 +43,9 @@ struct wenofd_batch {
   bool graph_tried = false;  // capture attempted for the current configuration
   long long cells = 0, launches = 0;
   double tuned_ms = 0.0;
+  // wenofd_batch_test_withhold: the next advance's first launch runs the
+  // withholding test instance with these (block, barrier); -1: not armed
+  int hold_block = -1, hold_barrier = -1;
 };
 
 namespace {
@@ -329,7 +332,24 @@ int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_
   for (int m = 0; m < b->n; ++m) before[m] = b->h_gather[m].steps;
   bool any_error = false;
   for (;;) {
-    if (int rc = launch_step_block(b)) return rc;
+    if (b->hold_block >= 0) {
+      // armed by wenofd_batch_test_withhold: one direct launch of the test
+      // instance, whose grid comes from its own occupancy
+      BatchArgs a = make_args(b, b->steps_per_launch);
+      a.hold_block = b->hold_block;
+      a.hold_barrier = b->hold_barrier;
+      b->hold_block = b->hold_barrier = -1;
+      BatchArgs q{};
+      int grid = 0;
+      BATCH_TRY(wenofd::launch_batch_fp64_withhold(q, b->stream, &grid));
+      BATCH_TRY(cudaMemsetAsync(b->d_counters, 0, size_t(b->steps_per_launch) * wenofd::kBatchPhases * sizeof(unsigned),
+                                b->stream));
+      BATCH_TRY(cudaMemsetAsync(b->d_barrier, 0, sizeof(unsigned), b->stream));
+      BATCH_TRY(wenofd::launch_batch_fp64_withhold(a, b->stream, &grid));
+      b->launches += 1;
+    } else if (int rc = launch_step_block(b)) {
+      return rc;
+    }
     BATCH_TRY(cudaMemcpyAsync(b->h_flags, b->d_flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     BATCH_TRY(cudaStreamSynchronize(b->stream));
     if (b->h_flags[0]) {
@@ -352,6 +372,22 @@ int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_
   if (any_error || first_err >= 0)
     return fail(WENOFD_NAN_DT, "Error: Timestep is not a number... (batch member " +
                                    std::to_string(first_err < 0 ? 0 : first_err) + ")");
+  return WENOFD_OK;
+}
+
+int wenofd_batch_test_withhold(wenofd_batch *b, int block, int barrier) {
+  if (!b) return fail(WENOFD_BAD_ARG, "null batch handle");
+  if (b->precision != WENOFD_FP64 || b->scheme != 1 || b->tile_i != 15)
+    return fail(WENOFD_BAD_ARG, "the withholding test instance is the FP64 WENO-Z batch kernel with tile 15");
+  if (block < 0 || barrier < 0) return fail(WENOFD_BAD_ARG, "block and barrier must be >= 0");
+  BATCH_TRY(cudaSetDevice(b->device));
+  BatchArgs q{};
+  int grid = 0;
+  BATCH_TRY(wenofd::launch_batch_fp64_withhold(q, b->stream, &grid));  // its grid (outside any capture)
+  if (block >= grid) return fail(WENOFD_BAD_ARG, "block must be below the test instance's grid of " +
+                                                     std::to_string(grid) + " blocks");
+  b->hold_block = block;
+  b->hold_barrier = barrier;
   return WENOFD_OK;
 }
 

@@ -42,6 +42,12 @@ cudaError_t launch_batch_fp64(const BatchArgs &b, int scheme, int tile_i, int bl
   return cudaErrorInvalidValue;
 }
 
+// With b.members null: attributes and grid of the test instance (its own
+// occupancy); else the cooperative launch on that grid.
+cudaError_t launch_batch_fp64_withhold(const BatchArgs &b, cudaStream_t s, int *grid) {
+  return dev::launch_batch_tile<double, 15, 256, true>(b, kWenoZ, 0, s, grid);
+}
+
 cudaError_t launch_batch_setup(BatchMember *members, int n, long long max_steps, cudaStream_t s) {
   k_batch_setup<<<(n + 127) / 128, 128, 0, s>>>(members, n, max_steps);
   return cudaGetLastError();

@@ -33,9 +33,12 @@ namespace dev {
 
 // Grid-wide barrier.  The block that arrives last runs last() with all its
 // threads before releasing the others; last() sees every write made before
-// the barrier.
-template <typename F>
-__device__ __forceinline__ void grid_barrier(const BatchArgs &b, F last) {
+// the barrier.  WITHHOLD (test instance only): block b.hold_block does not
+// arrive at the launch's barrier number b.hold_barrier (`index`), so every
+// block's wait there runs into the (short) poll limit.
+template <bool WITHHOLD = false, typename F>
+__device__ __forceinline__ void grid_barrier(const BatchArgs &b, F last, int index = 0) {
+  constexpr unsigned kLimit = WITHHOLD ? kBarrierTestLimit : kBarrierLimit;
   __shared__ int s_last;
   __shared__ unsigned s_gen;
   __syncthreads();
@@ -43,9 +46,11 @@ __device__ __forceinline__ void grid_barrier(const BatchArgs &b, F last) {
     volatile unsigned *gen = b.barrier + 1;
     s_gen = *gen;
     __threadfence();
-    const unsigned arrived = atomicAdd(b.barrier, 1u);
+    bool arrive = true;
+    if constexpr (WITHHOLD) arrive = !(int(blockIdx.x) == b.hold_block && index == b.hold_barrier);
+    const unsigned arrived = arrive ? atomicAdd(b.barrier, 1u) : 0u;
     __threadfence();
-    s_last = arrived == gridDim.x - 1;
+    s_last = arrive && arrived == gridDim.x - 1;
   }
   __syncthreads();
   if (s_last) {
@@ -65,7 +70,7 @@ __device__ __forceinline__ void grid_barrier(const BatchArgs &b, F last) {
     unsigned it = 0;
     while (*gen == s_gen) {
       ++it;
-      if (it > kBarrierLimit || ((it & 1023u) == 0u && *err)) {
+      if (it > kLimit || ((it & 1023u) == 0u && *err)) {
         atomicExch(b.error, 1);
         break;
       }
@@ -141,13 +146,15 @@ __device__ __forceinline__ int runnable(const Ctrl *c) {
   return (!__ldcg(&c->done) && !__ldcg(&c->error) && __ldcg(&c->steps) < __ldcg(&c->max_steps)) ? 1 : 0;
 }
 
-template <typename T, int SCHEME, int TI, int NT>
+template <typename T, int SCHEME, int TI, int NT, bool WITHHOLD = false>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) k_batch(BatchArgs b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BatchMember sM;
   constexpr int TJ = 32;
   constexpr bool F32 = sizeof(T) == 4;
   const int n = b.n;
+  int nbar = 0;  // barriers passed in this launch (the WITHHOLD hook's index)
+  auto barrier = [&](auto last) { grid_barrier<WITHHOLD>(b, last, nbar++); };
 
   // the loop condition of src/WENOFD.cpp:213, per member
   auto gate = [&]() {
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
     }
   };
 
-  grid_barrier(b, gate);
+  barrier(gate);
   for (int step = 0; step < b.nsteps; ++step) {
     unsigned *cnt = b.counters + step * kBatchPhases;
     // time-step reduction over each member's interior nodes
@@ -244,10 +251,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         for (int o = 16; o > 0; o >>= 1) lo = fmaxf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         if ((threadIdx.x & 31) == 0) atomicMax(&M.ctrl->screen_bits, __float_as_uint(lo));
       });
-      grid_barrier(b, Nothing());
+      barrier(Nothing());
     }
     for_member_items(b, cnt + 1, b.work.pt_prefix, sM, exact_pass);
-    grid_barrier(b, finalize);
+    barrier(finalize);
 
     // SSP-RK3: S -> A -> B -> S (src/WENOFD.cpp:352-396)
     for (int st = 0; st < 3; ++st) {
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         for (int e = first + int(threadIdx.x); e < first + kBcChunk && e < total; e += NT)
           bc_fill_entry(M.g, in, M.special, e);
       });
-      grid_barrier(b, Nothing());
+      barrier(Nothing());
       for_member_items(b, cnt + 3 + 2 * st, b.work.tile_prefix, sM, [&](int local, const BatchMember &M) {
         const int ti = local / M.tiles_j, tj = local - (local / M.tiles_j) * M.tiles_j;
         StageArgs a;
@@ -277,12 +284,12 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         else stage_tile_f64<SCHEME, TI, TJ, NT, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < 2) {
-        grid_barrier(b, Nothing());
+        barrier(Nothing());
       } else {
         // m_now += dt; count++ (src/WENOFD.cpp:213-224), then the next
         // step's gate; after the launch's last step, the host summary
         const bool last_step = step == b.nsteps - 1;
-        grid_barrier(b, [&]() {
+        barrier([&]() {
           int alive = 0, err = 0;
           for (int base = 0; base < n; base += NT) {
             const int m = base + int(threadIdx.x);
@@ -317,16 +324,21 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
 // resident blocks per SM (occupancy, or blocks_per_sm if smaller); call it
 // outside stream capture.  Otherwise launches *grid blocks, which must come
 // from that query.
-template <typename T, int TI, int NT>
+template <typename T, int TI, int NT, bool WITHHOLD = false>
 cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm, cudaStream_t s, int *grid) {
   constexpr size_t smem = stage_smem_bytes<T, TI, 32, false, NT>();
   void (*fn)(BatchArgs) = nullptr;
-  switch (scheme) {
-    case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT>; break;
-    case kWenoZ: fn = k_batch<T, kWenoZ, TI, NT>; break;
-    case kWenoZP: fn = k_batch<T, kWenoZP, TI, NT>; break;
-    case kWenoZPI: fn = k_batch<T, kWenoZPI, TI, NT>; break;
-    default: return cudaErrorInvalidValue;
+  if constexpr (WITHHOLD) {
+    if (scheme != kWenoZ) return cudaErrorInvalidValue;
+    fn = k_batch<T, kWenoZ, TI, NT, true>;
+  } else {
+    switch (scheme) {
+      case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT>; break;
+      case kWenoZ: fn = k_batch<T, kWenoZ, TI, NT>; break;
+      case kWenoZP: fn = k_batch<T, kWenoZP, TI, NT>; break;
+      case kWenoZPI: fn = k_batch<T, kWenoZPI, TI, NT>; break;
+      default: return cudaErrorInvalidValue;
+    }
   }
   if (!grid) return cudaErrorInvalidValue;
   cudaError_t e;

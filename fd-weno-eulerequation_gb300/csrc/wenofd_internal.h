@@ -107,6 +107,8 @@ constexpr int kBcChunk = 256;
 constexpr int kPtChunk = 4096;
 constexpr int kBatchPhases = 8;  // work counters per step: dt x 2, (bc, stage) x 3
 constexpr unsigned kBarrierLimit = 1u << 24;
+// Poll limit of the barrier in the withholding test instance (a few ms).
+constexpr unsigned kBarrierTestLimit = 1u << 12;
 
 struct BatchArgs {
   BatchMember *members;
@@ -117,6 +119,9 @@ struct BatchArgs {
   unsigned *barrier;   // [0] arrivals (zero before the launch), [1] generation
   int *error;          // set if a barrier wait gave up
   int *status;         // after the launch: [0] members that can still step, [1] any member error
+  // Test instance only (k_batch with WITHHOLD): block `hold_block` skips its
+  // arrival at the launch's barrier number `hold_barrier` (counted from 0).
+  int hold_block = -1, hold_barrier = -1;
 };
 
 // Per-member summary gathered for the host in one copy.
@@ -130,6 +135,11 @@ cudaError_t launch_batch_fp64(const BatchArgs &b, int scheme, int tile_i, int bl
                               int *grid);
 cudaError_t launch_batch_fp32(const BatchArgs &b, int scheme, int tile_i, int blocks_per_sm, cudaStream_t s,
                               int *grid);
+// The FP64 WENO-Z batched kernel (tile 15) built with the withholding test
+// hook and a short barrier poll limit: exercises the barrier's give-up path.
+// Never launched by wenofd_batch_advance unless wenofd_batch_test_withhold
+// armed it.
+cudaError_t launch_batch_fp64_withhold(const BatchArgs &b, cudaStream_t s, int *grid);
 cudaError_t launch_batch_setup(BatchMember *members, int n, long long max_steps, cudaStream_t s);
 cudaError_t launch_batch_gather(const BatchMember *members, int n, BatchMemberStatus *out, cudaStream_t s);
 

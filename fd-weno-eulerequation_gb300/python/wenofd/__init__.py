@@ -107,8 +107,9 @@ def lib() -> C.CDLL:
         L.wenofd_batch_autotune.argtypes = [H, C.c_int, P]
         L.wenofd_batch_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
         L.wenofd_batch_get_info.argtypes = [H, C.POINTER(BatchInfo)]
+        L.wenofd_batch_test_withhold.argtypes = [H, C.c_int, C.c_int]
         for f in ("wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
-                  "wenofd_batch_advance", "wenofd_batch_get_info"):
+                  "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold"):
             getattr(L, f).restype = C.c_int
         for f in ("wenofd_create", "wenofd_create_from_file", "wenofd_destroy", "wenofd_set_stream",
                   "wenofd_get_info", "wenofd_initialize", "wenofd_fill_boundary", "wenofd_set_state",
@@ -324,6 +325,10 @@ class Batch:
         _check(lib().wenofd_batch_get_info(self._h, C.byref(i)))
         return i
 
+    def test_withhold(self, block: int = 0, barrier: int = 1) -> None:
+        """Arm the barrier give-up test (wenofd_batch_test_withhold)."""
+        _check(lib().wenofd_batch_test_withhold(self._h, block, barrier))
+
 
 EXPORTED = [
     "wenofd_last_error", "wenofd_version", "wenofd_create", "wenofd_create_from_file", "wenofd_destroy",
@@ -335,7 +340,7 @@ EXPORTED = [
     "wenofd_routing_flags",
     "wenofd_indicator_data", "wenofd_mlp_forward", "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train",
     "wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
-    "wenofd_batch_advance", "wenofd_batch_get_info",
+    "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold",
 ]
 
 

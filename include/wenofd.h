@@ -246,6 +246,17 @@ int wenofd_batch_configure(wenofd_batch *b, int tile_i, int blocks_per_sm, int s
 int wenofd_batch_autotune(wenofd_batch *b, int steps, double *ms_per_step);
 int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_done);
 int wenofd_batch_get_info(const wenofd_batch *b, wenofd_batch_info *info);
+/* Test hook, no counterpart in the reference (whose failures abort,
+ * src/WENOFD.cpp:437-442): arms the next wenofd_batch_advance to run its
+ * first launch on a separately compiled instance of the batched kernel
+ * (FP64 WENO-Z batches, tile 15 only) whose grid barrier polls at most 4096
+ * times, and in which block `block` does not arrive at the launch's barrier
+ * number `barrier` (0 = the first).  Every wait at that barrier gives up,
+ * every later wait ends within 1024 polls, and the advance returns
+ * WENOFD_TIMEOUT; the members' states are then undefined and the batch can
+ * be advanced again after the members are re-initialised.  The kernels of
+ * the normal path carry no part of this hook. */
+int wenofd_batch_test_withhold(wenofd_batch *b, int block, int barrier);
 
 /* No counterpart in the reference.  calculateDeltaT (src/WENOFD.cpp:398-452
  * arithmetic, bit for bit) of a caller-owned device state, for callers that
@@ -254,8 +265,10 @@ int wenofd_batch_get_info(const wenofd_batch *b, wenofd_batch_info *info);
  * cannot absorb cudaMalloc/cudaFree, which synchronise the whole device.
  * Needs no handle and allocates nothing; it only enqueues two kernels.
  *   dev_state  interior state, device memory, float64 [4][nx][ny] (ej fastest)
- *   dev_dt     device double that receives dt, or NaN if a node's wave speed
- *              is NaN (where the reference aborts)
+ *   dev_dt     device double that receives dt, or NaN if any node's wave speed
+ *              is NaN.  This is stricter than the reference, whose loop
+ *              (src/WENOFD.cpp:426-442) lets a later finite node overwrite a
+ *              NaN candidate and aborts only when the last candidate is NaN.
  *   stream     cudaStream_t (NULL: the default stream); the call returns
  *              without waiting for the result.
  * Limit: nx*ny <= 2^28 nodes (16384 x 16384); larger grids are rejected with
@@ -263,7 +276,9 @@ int wenofd_batch_get_info(const wenofd_batch *b, wenofd_batch_info *info);
  * the library (per-block maxima), held by every GPU that loads the library
  * until exit.  The first call on a device looks up that array's address
  * (with the device current), so make it before any stream capture on that
- * device.  All calls share the array: calls that overlap on the GPU race. */
+ * device; so is the first call after a device reset (cudaDeviceReset), which
+ * looks the address up again.  All calls share the array: calls that
+ * overlap on the GPU race. */
 int wenofd_calc_dt_noalloc(const double *dev_state, int nx, int ny, double dx, double dy, double gamma,
                            double cfl, double now, double t_end, double *dev_dt, void *stream);
 

@@ -200,3 +200,48 @@ def test_batch_rejects_mixed_or_unsupported_members():
     finally:
         for s in (a, b, c, d, e):
             s.close()
+
+
+def test_barrier_give_up_reports_timeout_and_the_batch_recovers():
+    """The grid barrier's bounded wait: a test instance of the batched kernel
+    (short poll limit) in which block 0 withholds its arrival at the second
+    barrier of the launch.  Every block's wait there gives up, later waits end
+    quickly, the launch finishes and the host reports WENOFD_TIMEOUT; after the
+    members are re-initialised the same batch advances bit for bit like the
+    single solves."""
+    import time
+
+    cfgs = [_cfg(tc, nx, ny, seed, extra, wenofd.FP64) for tc, nx, ny, seed, extra in MEMBERS[:3]]
+    want = _alone(cfgs, 4)
+    solvers = [wenofd.Solver(c) for c in cfgs]
+    try:
+        for s in solvers:
+            s.initialize()
+        with wenofd.Batch(solvers) as b:
+            b.configure(tile_i=15, blocks_per_sm=0, steps_per_launch=2)
+            b.test_withhold(block=0, barrier=1)
+            t0 = time.perf_counter()
+            with pytest.raises(wenofd.WenofdError) as e:
+                b.advance(4)
+            assert e.value.status == wenofd.TIMEOUT
+            assert "barrier" in str(e.value)
+            assert time.perf_counter() - t0 < 30.0
+            for s in solvers:
+                s.initialize()
+            assert b.advance(4) == 4
+            for s, (U, now, _) in zip(solvers, want):
+                assert np.array_equal(s.get_state(), U)
+                assert s.info().now == now
+    finally:
+        for s in solvers:
+            s.close()
+
+
+def test_withhold_hook_rejects_other_batches():
+    cfgs = [_cfg(orc.RIEMANN_SEEDED, 40, 40, 1, {}, wenofd.FP32)]
+    with wenofd.Solver(cfgs[0]) as s:
+        s.initialize()
+        with wenofd.Batch([s]) as b:
+            with pytest.raises(wenofd.WenofdError) as e:
+                b.test_withhold(0, 1)
+            assert e.value.status == wenofd.BAD_ARG
