@@ -15,7 +15,11 @@
 // g_dt_block_max as a device address (on the host it names a stand-in), so
 // the first call on each device, with that device current, looks the address
 // up once with cudaGetSymbolAddress and caches it; that first call should
-// therefore come before any stream capture on that device.
+// therefore come before any stream capture on that device.  The cache is
+// keyed on the device's context as well: after cudaDeviceReset (or any
+// other teardown of the primary context) the module is loaded again and the
+// array may move, so the next call sees a new context id and looks the
+// address up again -- make that call, too, before any stream capture.
 //
 // Every call shares the one array and leaves its last contents behind.
 // Nothing in it has to start at zero: each call's first kernel writes every
@@ -23,6 +27,8 @@
 // streams, or from two threads, on the same device) race on the array.
 #include "../../include/wenofd.h"
 
+#include <cuda.h>  // CUresult, CUcontext and cuCtxGetId's type; no link to libcuda
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -40,6 +46,27 @@ static __device__ __align__(256) double g_dt_block_max[kMaxBlocks];
 
 std::mutex g_setup_mutex;
 double *g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};  // id of the context the address belongs to
+
+// Id of the calling thread's current context (cuCtxGetId, unique for the
+// life of the process: a context created after a reset gets a new one), 0
+// if none is current.  The driver function is reached through the runtime,
+// so the library does not link libcuda.
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_setup_mutex
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(fn);
+    looked_up = true;
+  }
+  unsigned long long id = 0;
+  if (!get_id || get_id(nullptr, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // Per node: s = lx/dx + ly/dy with lx = |u*1 + v*0| + c, ly = |u*0 + v*1| + c
 // (getMaxEigenValue(U, 1, 0) / (U, 0, 1), utils/equations.hpp:137-147), as
@@ -148,12 +175,18 @@ extern "C" int wenofd_calc_dt_noalloc(const double *dev_state, int nx, int ny, d
   double *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {  // once per device, with that device current
+    // Set-up: once per device (with that device current), and again when the
+    // device's context is not the one the cached address belongs to.  A
+    // thread with no current context yet reads id 0 and also sets up;
+    // cudaGetSymbolAddress makes the device's primary context current.
+    const unsigned long long ctx = current_context_id();
+    if (!g_scratch_ptr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_dt_block_max);
       if (e != cudaSuccess)
         return fail(WENOFD_CUDA_ERROR, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_scratch_ptr[dev] = static_cast<double *>(p);
+      g_scratch_ctx[dev] = current_context_id();
     }
     scratch = g_scratch_ptr[dev];
   }
