@@ -278,6 +278,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         a.dt = &M.ctrl->dt;
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
+        a.form = st == 0 ? kFormStage1 : (st == 1 ? kFormRK3Mid : kFormGeneric);
         a.flags = nullptr;
         if constexpr (F32)
           stage_tile_f32<SCHEME, TI, TJ, NT, false, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);

@@ -118,6 +118,7 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   args.dt = &s->ctrl->dt;
   args.active = &s->ctrl->active;
   args.mode = mode;
+  args.form = wenofd::rk_form(a, b, c, in, un);
   args.flags = s->precision == WENOFD_LEARNED ? s->flags : nullptr;
   if (bounds && s->tile_bounds) {
     args.bounds = s->tile_bounds;
@@ -720,6 +721,7 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
     for (const St &x : st) {
       StageArgs a{x.in, x.un, x.out, x.a, x.b, x.c, &s->ctrl->dt, &s->ctrl->active, wenofd::kModeRK,
                   s->precision == WENOFD_LEARNED ? s->flags : nullptr};
+      a.form = wenofd::rk_form(x.a, x.b, x.c, x.in, x.un);
       cudaError_t e = s->precision != WENOFD_FP64 ? wenofd::launch_stage_fp32(s->g, a, s->scheme, s->tile_i, s->stream)
                                                   : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
       CUDA_TRY(e);

@@ -73,8 +73,21 @@ struct StageArgs {
   // maximum lower bound (Ctrl::screen_bits).
   float2 *bounds = nullptr;
   unsigned *screen = nullptr;
+  // Which combination (a, b, c) is, from rk_form(): the FP32 tiles branch
+  // on this integer instead of comparing the FP64 coefficients on the
+  // device, where every FP64 compare issues on the 1/64-rate FP64 pipe.
+  int form = 0;
 };
 enum { kModeRK = 0, kModeRHS = 1 };
+// RK stage forms: a = 1, b = 0 on U^n itself (stage 1); SSP-RK3's middle
+// stage (3/4, 1/4, 1/4); RK2's second stage (1/2, 1/2, 1/2); any other.
+enum { kFormGeneric = 0, kFormStage1 = 1, kFormRK3Mid = 2, kFormRK2Mid = 3 };
+__host__ __device__ inline int rk_form(double a, double b, double c, const double *uin, const double *un) {
+  if (a == 1.0 && b == 0.0 && un == uin) return kFormStage1;
+  if (a == 0.75 && b == 0.25 && c == 0.25) return kFormRK3Mid;
+  if (a == 0.5 && b == 0.5 && c == 0.5) return kFormRK2Mid;
+  return kFormGeneric;
+}
 
 Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lambda, int bc_left,
                int bc_right, int bc_y, int gravity);
