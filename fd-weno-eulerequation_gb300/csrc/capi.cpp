@@ -98,6 +98,18 @@ int check_handle(const wenofd_solver *s) {
   return WENOFD_OK;
 }
 
+// Index of a state array in s->tma: 0 = S, 1 = A, 2 = B.
+int stage_buffer(const wenofd_solver *s, const double *in) { return in == s->A ? 1 : (in == s->B ? 2 : 0); }
+
+// After the stream has drained: TIMEOUT if a device wait gave up.
+int check_wait(wenofd_solver *s) {
+  if (!s->wait_error) return WENOFD_OK;
+  int err = 0;
+  CUDA_TRY(cudaMemcpy(&err, s->wait_error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return fail(WENOFD_TIMEOUT, "a bounded device wait gave up (stage TMA load or tensor-core completion)");
+  return WENOFD_OK;
+}
+
 int sync(wenofd_solver *s) {
   CUDA_TRY(cudaStreamSynchronize(s->stream));
   return WENOFD_OK;
@@ -129,13 +141,14 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   // The learned form classifies the nodes once per step, on the stage-1
   // input (ghosts just filled); all stages of the step route with those flags.
   if (s->precision == WENOFD_LEARNED && in == s->S && un == s->S && s->ind_ready) {
-    CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
+    CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->flags, s->wait_error,
                                       &s->ctrl->active, timeloop ? s->ctrl : nullptr, s->ind_interval,
                                       s->stream));
     s->launches += 1;
   }
   if (s->precision != WENOFD_FP64) {
-    CUDA_TRY(wenofd::launch_stage_fp32(s->g, args, s->scheme, s->tile_i, s->stream));
+    args.wait_error = s->wait_error;
+    CUDA_TRY(wenofd::launch_stage_fp32(s->g, args, s->tma[stage_buffer(s, in)], s->scheme, s->tile_i, s->stream));
   } else {
     CUDA_TRY(wenofd::launch_stage_fp64(s->g, args, s->scheme, s->tile_i, s->stream));
   }
@@ -232,7 +245,7 @@ void release(wenofd_solver *s) {
   cudaFree(s->ctrl);
   cudaFree(s->flags);
   cudaFree(s->ind_weights);
-  cudaFree(s->ind_error);
+  cudaFree(s->wait_error);
   cudaFree(s->tile_bounds);
   cudaFreeHost(s->ctrl_host);
   cudaFreeHost(s->red_host);
@@ -351,17 +364,24 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
     const size_t tiles = size_t((nx + 14) / 15) * size_t((ny + 31) / 32);
     ok = cudaMalloc(&s->tile_bounds, tiles * sizeof(float2)) == cudaSuccess;
   }
+  if (ok && precision != WENOFD_FP64)
+    ok = cudaMalloc(&s->wait_error, sizeof(int)) == cudaSuccess &&
+         cudaMemsetAsync(s->wait_error, 0, sizeof(int), s->stream) == cudaSuccess;
   if (ok && precision == WENOFD_LEARNED) {
     const size_t fb = size_t(s->g.nxt) * s->g.pitch;
     ok = cudaMalloc(&s->flags, fb) == cudaSuccess &&
          cudaMalloc(&s->ind_weights, wenofd::indicator_weights_bytes()) == cudaSuccess &&
-         cudaMalloc(&s->ind_error, sizeof(int)) == cudaSuccess &&
-         cudaMemsetAsync(s->flags, 1, fb, s->stream) == cudaSuccess &&
-         cudaMemsetAsync(s->ind_error, 0, sizeof(int), s->stream) == cudaSuccess;
+         cudaMemsetAsync(s->flags, 1, fb, s->stream) == cudaSuccess;
   }
   if (!ok) {
     cudaGetLastError();
     return bail(fail(WENOFD_CUDA_ERROR, "device allocation failed"));
+  }
+  if (precision != WENOFD_FP64) {  // TMA maps of the three stage inputs
+    double *bufs[3] = {s->S, s->A, s->B};
+    for (int k = 0; k < 3; ++k)
+      if ((e = wenofd::make_stage_tma(s->g, bufs[k], s->flags, tile_i, &s->tma[k])) != cudaSuccess)
+        return bail(fail(WENOFD_CUDA_ERROR, "cuTensorMapEncodeTiled failed for the stage tiles' TMA maps"));
   }
   ok = cudaMemsetAsync(s->S, 0, s->state_bytes, s->stream) == cudaSuccess &&
        cudaMemsetAsync(s->A, 0, s->state_bytes, s->stream) == cudaSuccess &&
@@ -548,7 +568,8 @@ int wenofd_get_flux(wenofd_solver *s, double *host_rhs) {
   if (int rc = launch_stage(s, s->S, s->S, s->A, 0.0, 0.0, 0.0, wenofd::kModeRHS)) return rc;
   if (host_rhs)
     if (int rc = download(s, s->A, host_rhs, cudaMemcpyDeviceToHost)) return rc;
-  return sync(s);
+  if (int rc = sync(s)) return rc;
+  return check_wait(s);
 }
 
 int wenofd_calc_dt(wenofd_solver *s, double *dt) {
@@ -570,7 +591,8 @@ int wenofd_rk_step(wenofd_solver *s, double dt) {
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_set_dt(s->ctrl, dt, s->stream));
   if (int rc = enqueue_rk(s)) return rc;
-  return sync(s);
+  if (int rc = sync(s)) return rc;
+  return check_wait(s);
 }
 
 int wenofd_step(wenofd_solver *s, double *dt_out) {
@@ -583,6 +605,7 @@ int wenofd_step(wenofd_solver *s, double *dt_out) {
   CUDA_TRY(wenofd::launch_step_end(s->ctrl, 0, s->stream));
   s->launches += 3;
   if (int rc = read_ctrl(s)) return rc;
+  if (int rc = check_wait(s)) return rc;
   if (s->ctrl_host->error) return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
   if (dt_out) *dt_out = s->ctrl_host->dt;
   return WENOFD_OK;
@@ -668,11 +691,7 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
     }
     if (int rc = read_ctrl(s)) return rc;
     const Ctrl &c = *s->ctrl_host;
-    if (s->ind_error) {
-      int err = 0;
-      CUDA_TRY(cudaMemcpy(&err, s->ind_error, sizeof(int), cudaMemcpyDeviceToHost));
-      if (err) return fail(WENOFD_TIMEOUT, "indicator kernel: a tensor-core completion wait gave up");
-    }
+    if (int rc = check_wait(s)) return rc;
     if (c.error) {
       if (steps_done) *steps_done = c.steps - start;
       return fail(WENOFD_NAN_DT, "Error: Timestep is not a number...");
@@ -722,8 +741,11 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
       StageArgs a{x.in, x.un, x.out, x.a, x.b, x.c, &s->ctrl->dt, &s->ctrl->active, wenofd::kModeRK,
                   s->precision == WENOFD_LEARNED ? s->flags : nullptr};
       a.form = wenofd::rk_form(x.a, x.b, x.c, x.in, x.un);
-      cudaError_t e = s->precision != WENOFD_FP64 ? wenofd::launch_stage_fp32(s->g, a, s->scheme, s->tile_i, s->stream)
-                                                  : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
+      a.wait_error = s->wait_error;
+      cudaError_t e = s->precision != WENOFD_FP64
+                          ? wenofd::launch_stage_fp32(s->g, a, s->tma[stage_buffer(s, x.in)], s->scheme, s->tile_i,
+                                                      s->stream)
+                          : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
       CUDA_TRY(e);
       s->launches += 1;
     }
@@ -734,7 +756,7 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms_per_launch = double(ms) / (double(reps) * st.size());
-  return WENOFD_OK;
+  return check_wait(s);
 }
 
 int wenofd_set_indicator(wenofd_solver *s, const float *host_params, float threshold) {
@@ -772,13 +794,13 @@ int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
   CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
-  CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->flags, s->ind_error,
+  CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->flags, s->wait_error,
                                     nullptr, nullptr, 1, s->stream));
   s->launches += 3;
   CUDA_TRY(cudaMemcpy2DAsync(host_flags, s->ny, s->flags + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost,
                              s->g.pitch, s->ny, s->nx, cudaMemcpyDeviceToHost, s->stream));
   int err = 0;
-  CUDA_TRY(cudaMemcpyAsync(&err, s->ind_error, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(&err, s->wait_error, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   if (int rc = sync(s)) return rc;
   if (err) return fail(WENOFD_TIMEOUT, "indicator kernel: a tensor-core completion wait gave up");
   return WENOFD_OK;

@@ -29,7 +29,8 @@ struct wenofd_solver {
   // learned form (PRECISION 2)
   unsigned char *flags = nullptr;  // [nxt][pitch], ghosts 1
   void *ind_weights = nullptr;     // packed BF16 indicator weights
-  int *ind_error = nullptr;
+  int *wait_error = nullptr;       // FP32 forms: set when a device wait (TMA load, tensor-core completion) gave up
+  wenofd::StageTma tma[3];         // FP32 forms: TMA maps of the stage inputs S, A, B (and the flags)
   float ind_logit_threshold = 0.0f;
   double label_deviation = 1e-2;  // LABEL_DEVIATION: training-label threshold
   int ind_interval = 1;            // INDICATOR_INTERVAL: steps per indicator run in the time loop

@@ -6,17 +6,20 @@
 // read is one 128-bit shared load per node instead of four, and the index
 // arithmetic is done once per node.
 //
-// Shared memory (float4 elements unless noted):
-//   Us   [HI][HJ]          state tile + 3-node halo (FP32)
+// Shared memory (float4 elements unless noted), from a 128-byte aligned base:
 //   Fp,Fm[HI][TJ] / [TI][HJ] split fluxes of the x / y sweep
 //   Hf   [TI+1][TJ] / [TI][TJ+1] face fluxes of the x / y sweep
+//   Us   [HI][HJ]          state tile + 3-node halo (FP32)
 //   U64  double [4][TI][TJ] the tile's FP64 input values (kept from the load)
 //   Un64 double [4][TI][TJ] the tile's FP64 U^n (stages 2-3, cp.async)
+// The TMA form lands the tile's FP64 halo box, [4][HI][40] doubles, at the
+// base, over Fp/Fm/Hf, which the sweeps write only after it is converted.
 #pragma once
 
 #include "aux_device.cuh"
 #include "convert.cuh"
 #include "physics.cuh"
+#include "tma.cuh"
 
 namespace wenofd {
 namespace dev {
@@ -32,7 +35,16 @@ struct StageSmem32 {
   static constexpr int kSplit = HI * TJ > TI * HJ ? HI * TJ : TI * HJ;
   static constexpr int kFace = (TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1);
   static constexpr int kKeep = KEEP ? 2 * 4 * TI * TJ : 0;  // doubles
-  static constexpr size_t bytes = sizeof(float4) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
+  // TMA halo box: 40 columns (the 38 halo columns from the even column
+  // before them) x HI rows x 4 planes of FP64; the flag box 48 x (TI + 4)
+  static constexpr int kBoxJ = 40, kFlagBoxJ = 48;
+  static constexpr unsigned kBoxBytes = 4u * HI * kBoxJ * 8u;
+  static constexpr unsigned kFlagBoxBytes = unsigned(kFlagBoxJ) * (TI + 4);
+  static_assert(kBoxBytes <= sizeof(float4) * (2 * kSplit + kFace), "halo box must fit over Fp, Fm and Hf");
+  static_assert(TJ + 6 <= kBoxJ && TJ + 8 <= kFlagBoxJ, "box widths");
+  // 128 bytes of slack: the base is rounded up to 128 bytes (TMA destination)
+  static constexpr size_t bytes =
+      128 + sizeof(float4) * (size_t(kU) + 2 * kSplit + kFace) + sizeof(double) * kKeep;
 };
 
 __device__ __forceinline__ float4 f4_split_store(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
@@ -203,27 +215,50 @@ __device__ __forceinline__ void cp_async_wait_all_f32() { asm volatile("cp.async
 // threads of the block.  ROUTE: faces take the linear upwind flux unless a
 // node of their stencil line is flagged (a.flags).  COH: inputs may have
 // been written earlier in the same launch by other blocks (persistent
-// batched kernel): loads through L2, U^n read in the epilogue.
+// batched kernel): loads through L2, U^n read in the epilogue.  TMA (the
+// per-solve kernels): the halo box and the flag box arrive by TMA (maps in
+// `tma`), one thread issuing both; otherwise every thread loads 128-bit
+// node pairs.
 // With a.bounds set (last stage of a step), the epilogue also screens the
 // time step of the nodes it writes (screen_speed) and stores the tile's
 // (max s32 - e, max s32 + e) at a.bounds[tile], raising *a.screen to the
 // tile's lower bound.
-template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false, bool KEEP = true>
+template <int SCHEME, int TI, int TJ, int NT, bool ROUTE, bool COH = false, bool KEEP = true, bool TMA = false>
 __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a, const int i0, const int j0,
-                                               unsigned char *smem_raw, const int tile = 0) {
+                                               unsigned char *smem_raw, const int tile = 0,
+                                               const StageTma *tma = nullptr) {
   using S = StageSmem32<TI, TJ, KEEP>;
   constexpr int HI = S::HI, HJ = S::HJ;
-  float4 *Us = reinterpret_cast<float4 *>(smem_raw);
-  float4 *Fp = Us + S::kU;
+  unsigned char *base = smem_raw + (((tma_smem_addr(smem_raw) + 127u) & ~127u) - tma_smem_addr(smem_raw));
+  float4 *Fp = reinterpret_cast<float4 *>(base);
   float4 *Fm = Fp + S::kSplit;
   float4 *Hf = Fm + S::kSplit;
-  double *U64 = reinterpret_cast<double *>(Hf + S::kFace);
+  float4 *Us = Hf + S::kFace;
+  double *U64 = reinterpret_cast<double *>(Us + S::kU);
   double *Un64 = U64 + 4 * TI * TJ;
   constexpr int FI = TI + 4, FJ = TJ + 4;
+  // node flags: flag node (fi, fj) at sflag[fi * FS + fj + FO]; the TMA box
+  // starts two columns before the first flag node
+  constexpr int FS = TMA ? S::kFlagBoxJ : FJ, FO = TMA ? 2 : 0;
   constexpr int kMaxFaces = S::kFace;
-  __shared__ unsigned char sflag[ROUTE ? FI * FJ : 1];
+  __shared__ __align__(128) unsigned char sflag[ROUTE ? FI * FS : 1];
   __shared__ short slist[ROUTE ? kMaxFaces : 1];
   __shared__ int scount;
+  __shared__ __align__(8) unsigned long long tma_bar;
+  if constexpr (TMA) {
+    // The halo box (and the flag box) by TMA, one thread issuing both.
+    if (threadIdx.x == 0) tma_bar_init(tma_smem_addr(&tma_bar), 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned bar = tma_smem_addr(&tma_bar);
+      tma_fence_proxy();
+      tma_bar_expect(bar, S::kBoxBytes + (ROUTE ? S::kFlagBoxBytes : 0u));
+      // box column 0 = ghosted column j0 (even: 16-byte aligned); row 0 =
+      // ghosted row 1 + i0, the first halo row
+      tma_load_3d(tma_smem_addr(base), &tma->u, j0, 1 + i0, 0, bar);
+      if constexpr (ROUTE) tma_load_2d(tma_smem_addr(sflag), &tma->flags, j0, 2 + i0, bar);
+    }
+  }
 
   const float gamma = g.gamma32, zpl = g.zpl32;
   const bool stage1 = a.form == kFormStage1;
@@ -240,6 +275,50 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     }
   }
 
+  if constexpr (TMA) {
+    // Bounded wait for the boxes; on give-up the whole block records the
+    // error and leaves the tile (a second bounded wait first lets a late
+    // copy land before the block exits).
+    const bool ok = tma_bar_wait(tma_smem_addr(&tma_bar), 0, kTmaWaitLimit);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        if (a.wait_error) atomicExch(a.wait_error, 1);
+        tma_bar_wait(tma_smem_addr(&tma_bar), 0, kTmaWaitLimit);
+      }
+      __syncthreads();
+      return;
+    }
+    // node pair p of halo row hi: box columns 2p, 2p + 1 = nodes hj = 2p - 1,
+    // 2p (20 pairs span the 38 halo columns; the first and last box column
+    // are not needed)
+    constexpr int PJ = S::kBoxJ / 2;
+    const double2 *box = reinterpret_cast<const double2 *>(base);
+    for (int t = threadIdx.x; t < HI * PJ; t += NT) {
+      const int hi = t / PJ, p = t - (t / PJ) * PJ;
+      double2 v[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) v[r] = box[(r * HI + hi) * PJ + p];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int hj = 2 * p - 1 + h;
+        if (hj < 0 || hj >= HJ) continue;
+        double x[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) x[r] = h ? v[r].y : v[r].x;
+        Us[hi * HJ + hj] = make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
+        if constexpr (KEEP) {
+          if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
+            const int q = (hi - 3) * TJ + hj - 3;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = x[r];
+          }
+        }
+      }
+    }
+    if constexpr (ROUTE) {
+      if (threadIdx.x == 0) scount = 0;
+    }
+  } else {
   // --- state tile with halo: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).
   // A thread loads a pair of adjacent nodes per component with one 128-bit
   // load: pair p of halo row hi covers global columns j0 + 2p and j0 + 2p + 1
@@ -319,6 +398,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       if (threadIdx.x == 0) scount = 0;
     }
   }
+  }  // TMA
   __syncthreads();
 
   // --- x sweep: split fluxes of halo rows 0..HI-1, tile columns
@@ -333,8 +413,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if (i0 + f > g.nx || j0 + j >= g.ny) continue;
     if constexpr (ROUTE) {
       Hf[t] = linear_face4(Fp + t, Fm + t + TJ, TJ);
-      const unsigned char *fl = sflag + f * FJ + (j + 2);  // nodes f-2 .. f+1
-      if (fl[0] | fl[FJ] | fl[2 * FJ] | fl[3 * FJ]) slist[atomicAdd(&scount, 1)] = short(t);
+      const unsigned char *fl = sflag + f * FS + (j + 2 + FO);  // nodes f-2 .. f+1
+      if (fl[0] | fl[FS] | fl[2 * FS] | fl[3 * FS]) slist[atomicAdd(&scount, 1)] = short(t);
     } else {
       Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
                                     Fm + t + TJ, TJ);
@@ -385,7 +465,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     const int s = i * HJ + f;
     if constexpr (ROUTE) {
       Hf[t] = linear_face4(Fp + s, Fm + s + 1, 1);
-      const unsigned char *fl = sflag + (i + 2) * FJ + f;  // nodes f-2 .. f+1 along y
+      const unsigned char *fl = sflag + (i + 2) * FS + f + FO;  // nodes f-2 .. f+1 along y
       if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount, 1)] = short(t);
     } else {
       Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,

@@ -7,10 +7,11 @@
 namespace wenofd {
 
 cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s) {
+  const StageTma none{};  // the FP64 tile loads its halo per thread
   switch (tile_i) {
     case 0:
-    case 15: return dev::launch_stage_tile<double, 15, 256>(g, a, scheme, s);
-    case 7: return dev::launch_stage_tile<double, 7, 256>(g, a, scheme, s);
+    case 15: return dev::launch_stage_tile<double, 15, 256>(g, a, none, scheme, s);
+    case 7: return dev::launch_stage_tile<double, 7, 256>(g, a, none, scheme, s);
   }
   return cudaErrorInvalidValue;
 }

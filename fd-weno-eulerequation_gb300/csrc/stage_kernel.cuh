@@ -210,14 +210,18 @@ __host__ __device__ constexpr bool stage_keeps_inputs() {
   return stage_blocks_per_sm<T, ROUTE, NT>() == 1;
 }
 
+// The FP32 tiles take their halo (and flags) by TMA through the maps in
+// `tma`; the FP64 tile ignores them.
 template <typename T, int SCHEME, int TI, int TJ, int NT, bool ROUTE>
-__global__ void __launch_bounds__(NT, stage_blocks_per_sm<T, ROUTE, NT>()) k_stage(Geom g, StageArgs a) {
+__global__ void __launch_bounds__(NT, stage_blocks_per_sm<T, ROUTE, NT>())
+    k_stage(Geom g, StageArgs a, const __grid_constant__ StageTma tma) {
   if (*a.active == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // first interior node of the tile (0-based)
   if constexpr (sizeof(T) == 4)
-    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, stage_keeps_inputs<T, ROUTE, NT>()>(
-        g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x));
+    stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, false, stage_keeps_inputs<T, ROUTE, NT>(), true>(
+        g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x),
+        &tma);
   else
     stage_tile_f64<SCHEME, TI, TJ, NT>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
 }
@@ -232,11 +236,11 @@ constexpr size_t stage_smem_bytes() {
 // Host-side launcher for one precision: picks the kernel instance for the
 // scheme and tile height, sets its shared-memory size, launches it.
 template <typename T, int TI, int NT, bool ROUTE = false>
-cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cudaStream_t s) {
+cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, const StageTma &tma, int scheme, cudaStream_t s) {
   constexpr int TJ = 32;
   constexpr size_t smem = stage_smem_bytes<T, TI, TJ, ROUTE, NT>();
   const dim3 grid((g.ny + TJ - 1) / TJ, (g.nx + TI - 1) / TI);
-  void (*fn)(Geom, StageArgs) = nullptr;
+  void (*fn)(Geom, StageArgs, StageTma) = nullptr;
   switch (scheme) {
     case kWenoJS: fn = k_stage<T, kWenoJS, TI, TJ, NT, ROUTE>; break;
     case kWenoZ: fn = k_stage<T, kWenoZ, TI, TJ, NT, ROUTE>; break;
@@ -257,7 +261,7 @@ cudaError_t launch_stage_tile(const Geom &g, const StageArgs &a, int scheme, cud
     if (e != cudaSuccess) return e;
     configured[scheme & 3] |= bit;
   }
-  fn<<<grid, NT, smem, s>>>(g, a);
+  fn<<<grid, NT, smem, s>>>(g, a, tma);
   return cudaGetLastError();
 }
 

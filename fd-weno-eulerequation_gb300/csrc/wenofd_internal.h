@@ -2,6 +2,7 @@
 // implementation.  Not installed; the public boundary is include/wenofd.h.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -77,7 +78,24 @@ struct StageArgs {
   // on this integer instead of comparing the FP64 coefficients on the
   // device, where every FP64 compare issues on the 1/64-rate FP64 pipe.
   int form = 0;
+  // FP32 per-solve tiles: set to 1 if a tile's TMA load wait gave up
+  // (the host reports WENOFD_TIMEOUT).
+  int *wait_error = nullptr;
 };
+
+// TMA descriptors of one FP32 stage launch: `u` tiles the input state
+// [4][nxt][pitch] FP64 in boxes of 40 columns x (TI + 6) rows x 4 planes
+// (the tile's 38 halo columns from an even, 16-byte aligned first column);
+// `flags` tiles the learned form's node flags [nxt][pitch] bytes in boxes of
+// 48 columns x (TI + 4) rows.
+struct StageTma {
+  CUtensorMap u;
+  CUtensorMap flags;
+};
+// Encodes the maps of one state array (and of the flag array, if not null)
+// for stage tiles of tile_i rows (15 or 31).
+cudaError_t make_stage_tma(const Geom &g, const double *state, const unsigned char *flags, int tile_i,
+                           StageTma *out);
 enum { kModeRK = 0, kModeRHS = 1 };
 // RK stage forms: a = 1, b = 0 on U^n itself (stage 1); SSP-RK3's middle
 // stage (3/4, 1/4, 1/4); RK2's second stage (1/2, 1/2, 1/2); any other.
@@ -95,7 +113,10 @@ Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lam
 // stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form,
 // routed by a.flags when it is set)
 cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
-cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
+// The FP32 tiles load their halo by TMA: `tma` holds the maps of a.uin (and
+// of a.flags) for tiles of tile_i rows.
+cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, const StageTma &tma, int scheme, int tile_i,
+                              cudaStream_t s);
 
 // batch_fp64.cu / batch_fp32.cu: the persistent batched kernel
 // (batch_kernel.cuh).  tile_i 0 = default; grid receives the launch's block
