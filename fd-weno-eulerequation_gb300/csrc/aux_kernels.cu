@@ -249,6 +249,30 @@ __global__ void k_copy_interior(Geom g, const double *src, double *dst, const in
 // kind 0: {max err, sum err, sum err^2} of density against the smooth case's
 // exact solution 1 + 0.2 sin(pi (x + y - t)) (utils/equations.hpp:438-439);
 // kind 1: sums of the four conserved variables.
+// getVitalVarVal (utils/equations.hpp:679-694) of every interior node: rho,
+// u, v, pre, c, E as planes k = 0..5 of nx x ny (j fastest), planes 0-3 at
+// out03, 4-5 at out45, each in the reference's operation order (this unit
+// has no multiply-add contraction).
+__global__ void k_output_vars(Geom g, const double *U, double *out03, double *out45) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
+    const long long k = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const double rho = U[k];
+    const double u = U[g.plane + k] / U[k];
+    const double v = U[2 * g.plane + k] / U[k];
+    const double E = U[3 * g.plane + k];
+    const double pre = (g.gamma - 1.0) * (E - 0.5 * rho * (u * u + v * v));
+    const double c = sqrt(g.gamma * pre / rho);
+    out03[t] = rho;
+    out03[n + t] = u;
+    out03[2 * n + t] = v;
+    out03[3 * n + t] = pre;
+    out45[t] = c;
+    out45[n + t] = E;
+  }
+}
+
 __global__ void k_reduce_blocks(Geom g, const double *U, int kind, double t, double xl, double yl,
                                 double *partials) {
   const long long n = (long long)g.nx * g.ny;
@@ -391,6 +415,11 @@ cudaError_t launch_copy_interior(const Geom &g, const double *src, double *dst, 
 }
 
 int reduce_blocks() { return kReduceBlocks; }
+
+cudaError_t launch_output_vars(const Geom &g, const double *U, double *out03, double *out45, cudaStream_t s) {
+  k_output_vars<<<grid_for((long long)g.nx * g.ny, 256), 256, 0, s>>>(g, U, out03, out45);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_reduce(const Geom &g, const double *U, int kind, double t, double xl, double yl,
                           double *partials, double *out, cudaStream_t s) {

@@ -815,6 +815,163 @@ int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *
   return sync(s);
 }
 
+int wenofd_output_variables(wenofd_solver *s, double *host_out) {
+  if (int rc = check_handle(s)) return rc;
+  if (!host_out) return fail(WENOFD_BAD_ARG, "null output");
+  CUDA_TRY(cudaSetDevice(s->device));
+  // The stage buffers are free between steps: planes 0-3 of the result go
+  // to A, planes 4-5 to B (each holds >= 4 * nx * ny doubles).
+  const size_t n = size_t(s->nx) * s->ny;
+  CUDA_TRY(wenofd::launch_output_vars(s->g, s->S, s->A, s->B, s->stream));
+  s->launches += 1;
+  CUDA_TRY(cudaMemcpyAsync(host_out, s->A, 4 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CUDA_TRY(cudaMemcpyAsync(host_out + 4 * n, s->B, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+namespace {
+
+// Restart file: this header, then the interior state [4][NX][NY] float64
+// (the host layout of wenofd_set_state), all little-endian.
+struct StateFileHeader {
+  char magic[8];  // "WENOFDS1"
+  int32_t version;
+  int32_t nx, ny, testcase, scheme, rk, precision;
+  int32_t reserved;
+  int64_t steps;
+  double now, t_end, dx, dy, gamma, cfl;
+};
+constexpr char kStateMagic[8] = {'W', 'E', 'N', 'O', 'F', 'D', 'S', '1'};
+
+// Sets the loop clock (time and step count) of the control block.
+int set_clock(wenofd_solver *s, double now, long long steps) {
+  CUDA_TRY(wenofd::launch_set_time(s->ctrl, now, s->stream));
+  if (int rc = read_ctrl(s)) return rc;
+  s->ctrl_host->steps = steps;
+  CUDA_TRY(cudaMemcpyAsync(s->ctrl, s->ctrl_host, sizeof(Ctrl), cudaMemcpyHostToDevice, s->stream));
+  return sync(s);
+}
+
+}  // namespace
+
+int wenofd_save_state(wenofd_solver *s, const char *path) {
+  if (int rc = check_handle(s)) return rc;
+  if (!path) return fail(WENOFD_BAD_ARG, "null path");
+  CUDA_TRY(cudaSetDevice(s->device));
+  if (int rc = read_ctrl(s)) return rc;
+  StateFileHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.version = 1;
+  h.nx = s->nx;
+  h.ny = s->ny;
+  h.testcase = s->testcase;
+  h.scheme = s->scheme;
+  h.rk = s->rk;
+  h.precision = s->precision;
+  h.steps = s->ctrl_host->steps;
+  h.now = s->ctrl_host->now;
+  h.t_end = s->ctrl_host->t_end;
+  h.dx = s->g.dx;
+  h.dy = s->g.dy;
+  h.gamma = s->g.gamma;
+  h.cfl = s->cfl;
+  std::vector<double> host(size_t(4) * s->nx * s->ny);
+  if (int rc = download(s, s->S, host.data(), cudaMemcpyDeviceToHost)) return rc;
+  if (int rc = sync(s)) return rc;
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(WENOFD_BAD_ARG, std::string("cannot write ") + path);
+  const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                  std::fwrite(host.data(), sizeof(double), host.size(), f) == host.size();
+  if (std::fclose(f) != 0 || !ok) return fail(WENOFD_BAD_ARG, std::string("write failed: ") + path);
+  return WENOFD_OK;
+}
+
+int wenofd_load_state(wenofd_solver *s, const char *path) {
+  if (int rc = check_handle(s)) return rc;
+  if (!path) return fail(WENOFD_BAD_ARG, "null path");
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return fail(WENOFD_BAD_ARG, std::string("cannot read ") + path);
+  StateFileHeader h{};
+  std::vector<double> host;
+  int rc = WENOFD_OK;
+  if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kStateMagic, 8) != 0 || h.version != 1) {
+    rc = fail(WENOFD_BAD_ARG, std::string("not a wenofd state file (version 1): ") + path);
+  } else if (h.nx != s->nx || h.ny != s->ny || h.testcase != s->testcase || h.dx != s->g.dx || h.dy != s->g.dy) {
+    rc = fail(WENOFD_BAD_CONFIG, "state file " + std::string(path) + " is for another grid or test case (" +
+                                     std::to_string(h.nx) + "x" + std::to_string(h.ny) + ", TESTCASE " +
+                                     std::to_string(h.testcase) + ")");
+  } else {
+    host.resize(size_t(4) * s->nx * s->ny);
+    if (std::fread(host.data(), sizeof(double), host.size(), f) != host.size())
+      rc = fail(WENOFD_BAD_ARG, std::string("state file is truncated: ") + path);
+  }
+  std::fclose(f);
+  if (rc) return rc;
+  CUDA_TRY(cudaSetDevice(s->device));
+  if ((rc = upload(s, host.data(), cudaMemcpyHostToDevice))) return rc;
+  return set_clock(s, h.now, h.steps);
+}
+
+int wenofd_indicator_sample(wenofd_solver *s, long long per_snapshot, unsigned long long seed, float *dev_x,
+                            float *dev_y, long long capacity, long long *rows_out) {
+  if (int rc = check_handle(s)) return rc;
+  if (!dev_x || !dev_y || !rows_out) return fail(WENOFD_BAD_ARG, "null output");
+  if (per_snapshot < 2 || capacity < 0) return fail(WENOFD_BAD_ARG, "per_snapshot must be >= 2, capacity >= 0");
+  CUDA_TRY(cudaSetDevice(s->device));
+  const long long n = (long long)s->nx * s->ny;
+  const int G = wenofd::sample_blocks();
+  // scratch in the stage buffer A (free between steps): labels, per-block
+  // counts and row offsets, the kept nodes' indices
+  const long long rows_cap = std::min(capacity, n);
+  auto align8 = [](size_t b) { return (b + 7) & ~size_t(7); };
+  const size_t off_counts = align8(size_t(n));
+  const size_t off_offsets = align8(off_counts + size_t(G) * sizeof(unsigned));
+  const size_t off_cells = off_offsets + size_t(G) * sizeof(long long);
+  if (off_cells + size_t(rows_cap) * sizeof(long long) > s->state_bytes)
+    return fail(WENOFD_BAD_ARG, "grid too small for the sampler's scratch");
+  unsigned char *scratch = reinterpret_cast<unsigned char *>(s->A);
+  unsigned char *labels = scratch;
+  unsigned *counts = reinterpret_cast<unsigned *>(scratch + off_counts);
+  long long *offsets = reinterpret_cast<long long *>(scratch + off_offsets);
+  long long *cells = reinterpret_cast<long long *>(scratch + off_cells);
+  unsigned long long *npos_dev = reinterpret_cast<unsigned long long *>(s->red_out);
+  CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
+  CUDA_TRY(wenofd::launch_labels(s->g, s->S, labels, s->label_deviation, s->stream));
+  CUDA_TRY(wenofd::launch_count_positive(labels, n, npos_dev, s->stream));
+  unsigned long long npos = 0;
+  CUDA_TRY(cudaMemcpyAsync(s->red_host, npos_dev, sizeof(npos), cudaMemcpyDeviceToHost, s->stream));
+  if (int rc = sync(s)) return rc;
+  std::memcpy(&npos, s->red_host, sizeof(npos));
+  const unsigned long long nneg = (unsigned long long)n - npos;
+  // half positives, half negatives where possible (the other class fills in)
+  const unsigned long long k_pos = std::min<unsigned long long>(npos, (unsigned long long)per_snapshot / 2);
+  const unsigned long long k_neg = std::min<unsigned long long>(nneg, (unsigned long long)per_snapshot - k_pos);
+  auto thr = [](unsigned long long k, unsigned long long count) -> unsigned long long {
+    if (count == 0 || k == 0) return 0ull;
+    if (k >= count) return 1ull << 32;
+    return (k << 32) / count;
+  };
+  const unsigned long long thr0 = thr(k_neg, nneg), thr1 = thr(k_pos, npos);
+  CUDA_TRY(wenofd::launch_sample_count(labels, n, seed, thr0, thr1, counts, s->stream));
+  std::vector<unsigned> hc(G);
+  CUDA_TRY(cudaMemcpyAsync(hc.data(), counts, size_t(G) * sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream));
+  if (int rc = sync(s)) return rc;
+  std::vector<long long> ho(G);
+  long long total = 0;
+  for (int b = 0; b < G; ++b) {
+    ho[b] = total;
+    total += hc[b];
+  }
+  CUDA_TRY(cudaMemcpyAsync(offsets, ho.data(), size_t(G) * sizeof(long long), cudaMemcpyHostToDevice, s->stream));
+  const long long rows = std::min(total, rows_cap);
+  CUDA_TRY(wenofd::launch_sample_write(s->g, s->S, labels, seed, thr0, thr1, offsets, rows_cap, rows, cells, dev_x,
+                                       dev_y, s->stream));
+  s->launches += 6;
+  if (int rc = sync(s)) return rc;
+  *rows_out = rows;
+  return WENOFD_OK;
+}
+
 int wenofd_conservation_sums(wenofd_solver *s, double out[4]) {
   if (int rc = check_handle(s)) return rc;
   if (!out) return fail(WENOFD_BAD_ARG, "null output");

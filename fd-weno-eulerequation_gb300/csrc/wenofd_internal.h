@@ -183,6 +183,22 @@ void pack_indicator_weights(const float *params, void *host_out);
 cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStream_t s);
 // labels: 1 where a face of the node has a WENO-Z weight deviation above `deviation`
 cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, double deviation, cudaStream_t s);
+// Balanced sampling of training nodes (wenofd_indicator_sample): positives
+// among `labels`; per-block kept counts (sample_blocks() entries) for
+// thresholds thr0 / thr1 (out of 2^32) on the negative / positive class;
+// then the kept nodes in node order from per-block row offsets: node index
+// into cells[row], label into y[row] (0.0 / 1.0), features into x[row][50]
+// (rows < capacity; `rows` = the number written).
+int sample_blocks();
+cudaError_t launch_count_positive(const unsigned char *labels, long long n, unsigned long long *count,
+                                  cudaStream_t s);
+cudaError_t launch_sample_count(const unsigned char *labels, long long n, unsigned long long seed,
+                                unsigned long long thr0, unsigned long long thr1, unsigned *block_count,
+                                cudaStream_t s);
+cudaError_t launch_sample_write(const Geom &g, const double *U, const unsigned char *labels, unsigned long long seed,
+                                unsigned long long thr0, unsigned long long thr1, const long long *offsets,
+                                long long capacity, long long rows, long long *cells, float *x, float *y,
+                                cudaStream_t s);
 // With ctrl set (the time loop), the indicator runs only on steps whose
 // count since Ctrl::ind_base is a multiple of `interval`; the flags of the
 // last run route the steps in between.
@@ -215,6 +231,10 @@ cudaError_t launch_copy_interior(const Geom &g, const double *src, double *dst, 
 // smooth case's exact solution at time t (xl, yl: domain origin);
 // kind 1: sums of the 4 conserved variables.
 int reduce_blocks();
+// outputAve's variables (rho, u, v, pre, c, E) of every interior node as
+// planes of nx * ny doubles (j fastest): planes 0-3 at out03, 4-5 at out45
+// (device), FP64 in the reference's order.
+cudaError_t launch_output_vars(const Geom &g, const double *U, double *out03, double *out45, cudaStream_t s);
 cudaError_t launch_reduce(const Geom &g, const double *U, int kind, double t, double xl, double yl,
                           double *partials, double *out, cudaStream_t s);
 

@@ -241,8 +241,12 @@ void CWENOFD::run(std::map<std::string, std::string> option) {
 }
 
 // outputAve, src/WENOFD.cpp:1161-1238: Tecplot ASCII, point data packing.
+// The variables (getVitalVarVal) come from the device
+// (wenofd_output_variables); the text is formatted here.
 void CWENOFD::outputAve(std::string prefix) {
-  downloadState();
+  const size_t plane = size_t(m_worldPointNumX) * m_worldPointNumY;
+  std::vector<double> vars(6 * plane);
+  check(wenofd_output_variables(m_handle, vars.data()), "wenofd_output_variables");
   std::string names[6];
   equation->getVitalVarName(names);
   std::ostringstream out;
@@ -250,14 +254,10 @@ void CWENOFD::outputAve(std::string prefix) {
       << "VARIABLES=X Y ";
   for (int k = 0; k < 6; ++k) out << names[k] << " ";
   out << "\nZONE T=TA, I=" << m_worldPointNumY << ", J=" << m_worldPointNumX << ", DATAPACKING=POINT\n";
-  const size_t plane = size_t(m_worldPointNumX) * m_worldPointNumY;
-  double q[4], vv[6];
   for (int i = 0; i < m_worldPointNumX; ++i)
     for (int j = 0; j < m_worldPointNumY; ++j) {
-      for (int r = 0; r < 4; ++r) q[r] = m_Uh[r * plane + size_t(i) * m_worldPointNumY + j];
-      equation->getVitalVarVal(q, vv);
       out << nodeX(i + m_ghostCellNum) << " " << nodeY(j + m_ghostCellNum) << " ";
-      for (int k = 0; k < 6; ++k) out << vv[k] << " ";
+      for (int k = 0; k < 6; ++k) out << vars[k * plane + size_t(i) * m_worldPointNumY + j] << " ";
       out << "\n";
     }
   const std::string filename = m_outputDir + "solution_" + prefix + ".plt";

@@ -108,6 +108,12 @@ def lib() -> C.CDLL:
         L.wenofd_batch_advance.argtypes = [H, C.c_longlong, C.POINTER(C.c_longlong)]
         L.wenofd_batch_get_info.argtypes = [H, C.POINTER(BatchInfo)]
         L.wenofd_batch_test_withhold.argtypes = [H, C.c_int, C.c_int]
+        L.wenofd_output_variables.argtypes = [H, P]
+        L.wenofd_indicator_sample.argtypes = [H, C.c_longlong, C.c_ulonglong, VP, VP, C.c_longlong,
+                                              C.POINTER(C.c_longlong)]
+        L.wenofd_mlp_init.argtypes = [C.POINTER(C.c_float), C.c_ulonglong]
+        L.wenofd_save_state.argtypes = [H, C.c_char_p]
+        L.wenofd_load_state.argtypes = [H, C.c_char_p]
         for f in ("wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
                   "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold"):
             getattr(L, f).restype = C.c_int
@@ -118,7 +124,8 @@ def lib() -> C.CDLL:
                   "wenofd_get_state_device", "wenofd_set_time", "wenofd_rk_step", "wenofd_advance",
                   "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
                   "wenofd_set_indicator", "wenofd_indicator_flags", "wenofd_routing_flags", "wenofd_indicator_data",
-                  "wenofd_mlp_forward",
+                  "wenofd_mlp_forward", "wenofd_output_variables", "wenofd_save_state", "wenofd_load_state",
+                  "wenofd_indicator_sample", "wenofd_mlp_init",
                   "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train"):
             getattr(L, f).restype = C.c_int
         _lib = L
@@ -279,6 +286,27 @@ class Solver:
         _check(lib().wenofd_conservation_sums(self._h, _dptr(out)))
         return out
 
+    def output_variables(self) -> np.ndarray:
+        """outputAve's (rho, u, v, pre, c, E), (6, NX, NY), computed on the device."""
+        i = self.info()
+        out = np.zeros((6, i.nx, i.ny))
+        _check(lib().wenofd_output_variables(self._h, _dptr(out)))
+        return out
+
+    def indicator_sample(self, per_snapshot: int, seed: int, x_ptr: int, y_ptr: int, capacity: int) -> int:
+        """Balanced device-side training sample of the current state
+        (wenofd_indicator_sample); returns the rows written."""
+        rows = C.c_longlong()
+        _check(lib().wenofd_indicator_sample(self._h, per_snapshot, seed, C.c_void_p(x_ptr), C.c_void_p(y_ptr),
+                                             capacity, C.byref(rows)))
+        return rows.value
+
+    def save_state(self, path: str) -> None:
+        _check(lib().wenofd_save_state(self._h, os.fsencode(path)))
+
+    def load_state(self, path: str) -> None:
+        _check(lib().wenofd_load_state(self._h, os.fsencode(path)))
+
 
 class Batch:
     """Many Solver handles advanced together by one persistent kernel
@@ -340,8 +368,16 @@ EXPORTED = [
     "wenofd_routing_flags",
     "wenofd_indicator_data", "wenofd_mlp_forward", "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train",
     "wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
-    "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold",
+    "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold", "wenofd_output_variables",
+    "wenofd_save_state", "wenofd_load_state", "wenofd_indicator_sample", "wenofd_mlp_init",
 ]
+
+
+def mlp_init(seed: int) -> np.ndarray:
+    """Initial network parameters (wenofd_mlp_init, host only)."""
+    out = np.zeros(MLP_PARAMS, dtype=np.float32)
+    _check(lib().wenofd_mlp_init(out.ctypes.data_as(C.POINTER(C.c_float)), seed))
+    return out
 
 
 def mlp_forward(params_ptr: int, x_ptr: int, n: int, logits_ptr: int, stream: int = 0) -> None:

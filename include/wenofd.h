@@ -146,6 +146,23 @@ int wenofd_error_norms(wenofd_solver *s, double out[3]);
  * column of the state). */
 int wenofd_conservation_sums(wenofd_solver *s, double out[4]);
 
+/* CWENOFD::outputAve's variables (utils/equations.hpp:666-698,
+ * src/WENOFD.cpp:1161-1238) of the current state, computed on the device in
+ * FP64 with the reference's operation order: host_out receives
+ * [6][NX][NY] doubles, planes rho, u, v, pre, c, E (the Tecplot VARIABLES
+ * after X and Y).  Uses the stage buffers as scratch (between steps). */
+int wenofd_output_variables(wenofd_solver *s, double *host_out);
+/* Binary restart, no counterpart in the reference (its outputs are Tecplot
+ * text).  wenofd_save_state writes a 96-byte header -- magic "WENOFDS1",
+ * version 1, NX, NY, TESTCASE, SCHEME, RKMETH, PRECISION, step count, time,
+ * TEND, dx, dy, gamma, CFL -- and the interior state [4][NX][NY] float64,
+ * all little-endian.  wenofd_load_state reads such a file into a handle of
+ * the same grid and TESTCASE (else WENOFD_BAD_CONFIG) and sets its state,
+ * time and step count; a run continued from it is bit for bit the run that
+ * wrote it. */
+int wenofd_save_state(wenofd_solver *s, const char *path);
+int wenofd_load_state(wenofd_solver *s, const char *path);
+
 /* Measurement aid, no reference counterpart: replays the RK stage kernels of
  * one step (RKMETH's stages, boundary fills excluded, dt as last set) `reps`
  * times on the handle's stream between two CUDA events and returns the mean
@@ -180,16 +197,30 @@ int wenofd_routing_flags(wenofd_solver *s, unsigned char *host_flags);
  * ones by more than LABEL_DEVIATION, default 1e-2, on a non-flat stencil at
  * any of the node's four faces), device pointers; either may be NULL. */
 int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *dev_labels);
+/* Balanced training sample of the current state, formed on the device:
+ * labels of every node as wenofd_indicator_data forms them, then about
+ * per_snapshot / 2 flagged and per_snapshot / 2 unflagged nodes (fewer of a
+ * class that has fewer; the other class fills in), each node of a class kept
+ * independently when a hash of (seed, node index) falls below that class's
+ * rate; the same state and seed keep the same nodes.  The kept nodes'
+ * features go to dev_x[row][50] and their labels (0.0 / 1.0) to dev_y[row],
+ * rows in node order, at most `capacity` rows; *rows_out receives the count
+ * (it varies around per_snapshot by the sampling).  Synchronous.  Replaces
+ * the host-side sampling a training driver would otherwise need. */
+int wenofd_indicator_sample(wenofd_solver *s, long long per_snapshot, unsigned long long seed, float *dev_x,
+                            float *dev_y, long long capacity, long long *rows_out);
 /* FP32 training kernels on device buffers (stream-ordered):
  *   forward: logits[n] of samples x[n][50];
  *   backward: mean binary cross-entropy of logits vs y[n] (0/1) into *loss and
  *             its gradient into grad[WENOFD_MLP_PARAMS] (both overwritten);
  *   adam: one Adam step (beta 0.9 / 0.999, eps 1e-8), step counts from 1;
- *   train: epochs of shuffled mini-batches of backward + adam, the mean loss
- *          of each epoch to host_epoch_loss[epochs] (may be NULL); each
- *          mini-batch's gradient is summed in a fixed order, so the same
- *          data and seed give the same parameters bit for bit (the
- *          standalone backward accumulates with atomics). */
+ *   train: per epoch a seeded random permutation of the n samples, cut
+ *          into mini-batches of backward + adam (the samples may come in
+ *          any order), the mean loss of each epoch to host_epoch_loss[epochs]
+ *          (may be NULL); each mini-batch's gradient is summed in a fixed
+ *          order, so the same data and seed give the same parameters bit for
+ *          bit (the standalone backward accumulates with atomics).  It
+ *          allocates its optimiser state and an 8-byte index per sample. */
 int wenofd_mlp_forward(const float *dev_params, const float *dev_x, long long n, float *dev_logits, void *stream);
 int wenofd_mlp_backward(const float *dev_params, const float *dev_x, const float *dev_y, long long n,
                         float *dev_grad, float *dev_loss, void *stream);
@@ -197,6 +228,11 @@ int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *dev_m, floa
                     void *stream);
 int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs, int batch,
                      float lr, unsigned long long seed, float *host_epoch_loss, void *stream);
+/* Initial parameters for training (host buffer of WENOFD_MLP_PARAMS floats,
+ * host-only, no GPU needed): W1 uniform in +-sqrt(6/50), W2 and w3 uniform
+ * in +-sqrt(6/32), biases zero, from a seeded splitmix64 sequence; the same
+ * seed gives the same parameters everywhere. */
+int wenofd_mlp_init(float *host_params, unsigned long long seed);
 
 /* ---- Batches: many independent solves in one persistent launch ----------
  * No counterpart in the reference, which runs one solve per program
