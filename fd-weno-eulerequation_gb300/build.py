@@ -48,6 +48,7 @@ CXX_UNITS = ["capi.cpp", "cases.cpp", "batch.cpp"]
 
 LIB = os.path.join(OUT, "libwenofd.so")
 EXE = os.path.join(OUT, "wenofd")
+TRAIN_EXE = os.path.join(OUT, "wenofd_train")
 
 
 def _deps() -> list[str]:
@@ -110,6 +111,14 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
             os.path.getmtime(p) > os.path.getmtime(EXE) for p in host_srcs + [LIB, os.path.join(HOST, "WENOFD.hpp")])):
         _run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I" + os.path.join(ROOT, "include"),
               "-I" + HOST] + host_srcs + ["-L" + OUT, "-lwenofd", "-Wl,-rpath,$ORIGIN", "-o", EXE])
+    # the indicator's C-ABI training driver (no Python involved)
+    train_src = os.path.join(HOST, "train_indicator.cpp")
+    if force or not os.path.exists(TRAIN_EXE) or any(
+            os.path.getmtime(p) > os.path.getmtime(TRAIN_EXE) for p in (train_src, LIB)):
+        lib_dir = os.path.join(CUDA_HOME, "lib64")
+        _run([cxx, "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
+              "-I" + os.path.join(CUDA_HOME, "include"), train_src, "-L" + OUT, "-lwenofd", "-L" + lib_dir,
+              "-lcudart", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + lib_dir, "-o", TRAIN_EXE])
     return "".join(log)
 
 

@@ -11,11 +11,13 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "../../include/wenofd.h"
+
 #include "learned_common.cuh"
 
 namespace wenofd {
@@ -51,8 +53,10 @@ __global__ void k_mlp_forward(const float *P, const float *X, long long n, float
 // given `part`, writes them to its own row there for an ordered sum.
 constexpr int kBB = 128;
 
+// rows: with idx set, sample s of the mini-batch is row idx[s] of X and Y.
 __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const float *X, const float *Y, long long n,
-                                                      float inv_n, float *grad, float *loss, float *part) {
+                                                      float inv_n, float *grad, float *loss, float *part,
+                                                      const long long *idx) {
   extern __shared__ float sm[];
   float *sp = sm;                  // kParams
   float *sx = sp + kParams;        // kBB * kIn
@@ -66,7 +70,9 @@ __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const floa
   const long long s0 = (long long)blockIdx.x * kBB;
   for (int k = threadIdx.x; k < kBB * kIn; k += kBB) {
     const long long s = s0 + k / kIn;
-    sx[k] = s < n ? X[s0 * kIn + k] : 0.0f;
+    if (s >= n) sx[k] = 0.0f;
+    else if (idx) sx[k] = X[idx[s] * kIn + (k - (k / kIn) * kIn)];
+    else sx[k] = X[s0 * kIn + k];
   }
   __syncthreads();
   const int t = threadIdx.x;
@@ -89,7 +95,7 @@ __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const floa
     sh2[t * kHid + o] = h;
     logit += sp[oW3 + o] * h;
   }
-  const float y = valid ? Y[s0 + t] : 0.0f;
+  const float y = valid ? Y[idx ? idx[s0 + t] : s0 + t] : 0.0f;
   const float pr = 1.0f / (1.0f + expf(-logit));
   const float d = valid ? (pr - y) * inv_n : 0.0f;
   sd[t] = d;
@@ -590,6 +596,34 @@ cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights
 
 // ------------------------------------------------------------- C ABI
 
+namespace wenofd {
+void set_last_error(const std::string &msg);  // capi.cpp: the text wenofd_last_error() returns
+}
+
+// He-uniform initial parameters from a seeded splitmix64 sequence: W1 from
+// U(-1, 1) * sqrt(6 / 50), W2 and w3 from U(-1, 1) * sqrt(6 / 32), biases 0.
+// Host only; the same seed gives the same parameters on any machine.
+extern "C" int wenofd_mlp_init(float *host_params, unsigned long long seed) {
+  if (!host_params) {
+    wenofd::set_last_error("null parameter buffer");
+    return WENOFD_BAD_ARG;
+  }
+  unsigned long long st = seed;
+  auto uniform = [&st]() {  // in [-1, 1)
+    unsigned long long z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return 2.0 * double(z >> 11) * (1.0 / 9007199254740992.0) - 1.0;
+  };
+  for (int k = 0; k < wenofd::lrn::kParams; ++k) host_params[k] = 0.0f;
+  const double s1 = std::sqrt(6.0 / 50.0), s2 = std::sqrt(6.0 / 32.0);
+  for (int k = 0; k < wenofd::lrn::oB1; ++k) host_params[wenofd::lrn::oW1 + k] = float(uniform() * s1);
+  for (int k = 0; k < wenofd::lrn::oB2 - wenofd::lrn::oW2; ++k) host_params[wenofd::lrn::oW2 + k] = float(uniform() * s2);
+  for (int k = 0; k < wenofd::lrn::oB3 - wenofd::lrn::oW3; ++k) host_params[wenofd::lrn::oW3 + k] = float(uniform() * s2);
+  return WENOFD_OK;
+}
+
 extern "C" int wenofd_mlp_forward(const float *dev_params, const float *dev_x, long long n, float *dev_logits,
                                   void *stream) {
   if (!dev_params || !dev_x || !dev_logits || n < 0) return WENOFD_BAD_ARG;
@@ -606,7 +640,7 @@ namespace {
 // (room for one row of kParams + 1 floats per block) they write partials and
 // k_grad_reduce sums them in block order.
 int launch_backward(const float *params, const float *x, const float *y, long long n, float *grad, float *loss,
-                    float *part, cudaStream_t s) {
+                    float *part, cudaStream_t s, const long long *idx = nullptr) {
   using namespace wenofd::lrn;
   const size_t smem = sizeof(float) * (kParams + kBB * kIn + 4 * kBB * kHid + 2 * kBB);
   int dev = 0;
@@ -622,7 +656,7 @@ int launch_backward(const float *params, const float *x, const float *y, long lo
   if (!part && (cudaMemsetAsync(grad, 0, kParams * sizeof(float), s) != cudaSuccess ||
                 cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess))
     return WENOFD_CUDA_ERROR;
-  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(params, x, y, n, 1.0f / float(n), grad, loss, part);
+  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(params, x, y, n, 1.0f / float(n), grad, loss, part, idx);
   if (part) k_grad_reduce<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(part, int(blocks), grad, loss);
   return cudaGetLastError() == cudaSuccess ? WENOFD_OK : WENOFD_CUDA_ERROR;
 }
@@ -643,11 +677,12 @@ extern "C" int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *
   return cudaGetLastError() == cudaSuccess ? WENOFD_OK : WENOFD_CUDA_ERROR;
 }
 
-// Training loop: per epoch a seeded shuffle of the mini-batch order, and per
-// mini-batch one backward pass and one Adam step.  The epoch's mean loss is
-// read back once per epoch.  Each mini-batch's gradient is summed in block
-// order (k_grad_reduce), so the same data and seed give the same parameters
-// bit for bit.
+// Training loop: per epoch a seeded permutation of the samples (so the data
+// may come in any order, e.g. grouped by snapshot and node), cut into
+// mini-batches, and per mini-batch one backward pass and one Adam step.  The
+// epoch's mean loss is estimated from every 16th mini-batch's loss.  Each
+// mini-batch's gradient is summed in block order (k_grad_reduce), so the same
+// data and seed give the same parameters bit for bit.
 extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs,
                                 int batch, float lr, unsigned long long seed, float *host_epoch_loss, void *stream) {
   using namespace wenofd::lrn;
@@ -656,32 +691,43 @@ extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const flo
   // grad | m | v | loss | epoch loss | the backward blocks' partial rows
   const long long part_rows = (std::min<long long>(batch, n) + kBB - 1) / kBB;
   float *buf = nullptr;
+  long long *perm_dev = nullptr;
   if (cudaMalloc(&buf, sizeof(float) * (3 * kParams + 2 + part_rows * (kParams + 1))) != cudaSuccess)
     return WENOFD_CUDA_ERROR;
+  if (cudaMalloc(&perm_dev, sizeof(long long) * size_t(n)) != cudaSuccess) {
+    cudaFree(buf);
+    return WENOFD_CUDA_ERROR;
+  }
   float *grad = buf, *m = buf + kParams, *v = buf + 2 * kParams, *loss = buf + 3 * kParams;
   float *part = buf + 3 * kParams + 2;
   int rc = WENOFD_OK;
   if (cudaMemsetAsync(m, 0, sizeof(float) * 2 * kParams, s) != cudaSuccess) rc = WENOFD_CUDA_ERROR;
   const long long nb = (n + batch - 1) / batch;
-  std::vector<long long> order(nb);
-  for (long long b = 0; b < nb; ++b) order[b] = b;
+  std::vector<long long> perm(n);
+  for (long long r = 0; r < n; ++r) perm[r] = r;
   unsigned long long st = seed ? seed : 0x9E3779B97F4A7C15ULL;
   int step = 0;
   for (int e = 0; e < epochs && rc == WENOFD_OK; ++e) {
-    for (long long b = nb - 1; b > 0; --b) {  // Fisher-Yates with splitmix64
+    for (long long r = n - 1; r > 0; --r) {  // Fisher-Yates with splitmix64
       unsigned long long z = (st += 0x9E3779B97F4A7C15ULL);
       z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
       z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
       z ^= z >> 31;
-      std::swap(order[b], order[z % (unsigned long long)(b + 1)]);
+      std::swap(perm[r], perm[z % (unsigned long long)(r + 1)]);
     }
+    // the previous epoch's mini-batches read the permutation buffer: copy
+    // after they ran (same stream; the copy from pageable memory returns
+    // once the host buffer is staged)
+    if (cudaMemcpyAsync(perm_dev, perm.data(), sizeof(long long) * size_t(n), cudaMemcpyHostToDevice, s) !=
+        cudaSuccess)
+      rc = WENOFD_CUDA_ERROR;
     // the loss of every 16th mini-batch (and the last) estimates the epoch's mean
     double epoch_loss = 0.0;
     int sampled = 0;
     for (long long k = 0; k < nb && rc == WENOFD_OK; ++k) {
-      const long long off = order[k] * batch;
+      const long long off = k * batch;
       const long long cnt = off + batch <= n ? batch : n - off;
-      rc = launch_backward(dev_params, dev_x + off * kIn, dev_y + off, cnt, grad, loss, part, s);
+      rc = launch_backward(dev_params, dev_x, dev_y, cnt, grad, loss, part, s, perm_dev + off);
       if (rc == WENOFD_OK) rc = wenofd_mlp_adam(dev_params, grad, m, v, ++step, lr, stream);
       if (rc == WENOFD_OK && host_epoch_loss && (k == nb - 1 || k % 16 == 0)) {
         float l = 0.0f;
@@ -696,5 +742,6 @@ extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const flo
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) rc = WENOFD_CUDA_ERROR;
   cudaFree(buf);
+  cudaFree(perm_dev);
   return rc;
 }

@@ -13,10 +13,10 @@ namespace lrn {
 
 // ------------------------------------------------------------- features
 
-__global__ void k_features(Geom g, const double *U, float *feat) {
-  const long long n = (long long)g.nx * g.ny;
+// The 50 features of interior node c (index i * ny + j) into row[0..49].
+__device__ __forceinline__ void cell_features(const Geom &g, const double *U, long long c, float *row) {
   const float gam = float(g.gamma);
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+  {
     const int i = int(c / g.ny), j = int(c - (c / g.ny) * g.ny);
     float wr[25], wp[25];
     for (int a = 0; a < 5; ++a)
@@ -29,10 +29,90 @@ __global__ void k_features(Geom g, const double *U, float *feat) {
       }
     float o[25];
     normalise(wr, o);
-    for (int k = 0; k < 25; ++k) feat[c * kIn + k] = o[k];
+    for (int k = 0; k < 25; ++k) row[k] = o[k];
     normalise(wp, o);
-    for (int k = 0; k < 25; ++k) feat[c * kIn + 25 + k] = o[k];
+    for (int k = 0; k < 25; ++k) row[25 + k] = o[k];
   }
+}
+
+__global__ void k_features(Geom g, const double *U, float *feat) {
+  const long long n = (long long)g.nx * g.ny;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+    cell_features(g, U, c, feat + c * kIn);
+}
+
+// ----------------------------------------------------- balanced sampling
+//
+// wenofd_indicator_sample: every node of class y (its label) is kept when a
+// 32-bit hash of (seed, node) lies below thr[y] = k_y / count_y * 2^32, so
+// about k_y nodes of each class are kept, independently, and the same seed
+// keeps the same nodes.  Kept nodes are written in node order: block b of
+// kSampleBlocks scans the contiguous node range [b * R, (b + 1) * R).
+
+constexpr int kSampleBlocks = 1024, kSampleThreads = 256;
+
+__device__ __forceinline__ unsigned sample_hash(unsigned long long seed, long long node) {
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(node + 1);  // splitmix64
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return unsigned(z >> 32);
+}
+
+__device__ __forceinline__ bool sample_keep(const unsigned char *labels, long long c, unsigned long long seed,
+                                            unsigned long long thr0, unsigned long long thr1) {
+  return (unsigned long long)sample_hash(seed, c) < (labels[c] ? thr1 : thr0);
+}
+
+__global__ void k_count_positive(const unsigned char *labels, long long n, unsigned long long *count) {
+  unsigned local = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+    local += labels[c] ? 1u : 0u;
+  local = __reduce_add_sync(0xffffffffu, local);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, (unsigned long long)local);
+}
+
+// Pass 1: kept nodes per block.  Pass 2 (offsets[b] = kept nodes of the
+// blocks before b): each kept node's output row, in node order; rows past
+// `capacity` are dropped.
+template <bool WRITE>
+__global__ void k_sample_pass(const unsigned char *labels, long long n, unsigned long long seed,
+                              unsigned long long thr0, unsigned long long thr1, unsigned *block_count,
+                              const long long *offsets, long long capacity, long long *cells, float *y) {
+  __shared__ unsigned warp_total[kSampleThreads / 32];
+  const long long per = (n + kSampleBlocks - 1) / kSampleBlocks;
+  const long long first = blockIdx.x * per, last = first + per < n ? first + per : n;
+  long long base = WRITE ? offsets[blockIdx.x] : 0;
+  unsigned kept = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (long long c0 = first; c0 < last; c0 += kSampleThreads) {
+    const long long c = c0 + threadIdx.x;
+    const bool keep = c < last && sample_keep(labels, c, seed, thr0, thr1);
+    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_total[warp] = __popc(ballot);
+    __syncthreads();
+    unsigned before = __popc(ballot & ((1u << lane) - 1u)), chunk = 0;
+    for (int w = 0; w < kSampleThreads / 32; ++w) {
+      if (w < warp) before += warp_total[w];
+      chunk += warp_total[w];
+    }
+    if (WRITE && keep) {
+      const long long row = base + before;
+      if (row < capacity) {
+        cells[row] = c;
+        y[row] = labels[c] ? 1.0f : 0.0f;
+      }
+    }
+    base += chunk;
+    kept += chunk;
+    __syncthreads();
+  }
+  if (!WRITE && threadIdx.x == 0) block_count[blockIdx.x] = kept;
+}
+
+__global__ void k_features_of(Geom g, const double *U, const long long *cells, long long rows, float *feat) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x)
+    cell_features(g, U, cells[r], feat + r * kIn);
 }
 
 // --------------------------------------------------------------- labels
@@ -124,6 +204,36 @@ cudaError_t launch_features(const Geom &g, const double *U, float *feat, cudaStr
 
 cudaError_t launch_labels(const Geom &g, const double *U, unsigned char *labels, double deviation, cudaStream_t s) {
   lrn::k_labels<<<lrn::grid_for((long long)g.nx * g.ny, 128, 152 * 32), 128, 0, s>>>(g, U, labels, deviation);
+  return cudaGetLastError();
+}
+
+int sample_blocks() { return lrn::kSampleBlocks; }
+
+cudaError_t launch_count_positive(const unsigned char *labels, long long n, unsigned long long *count,
+                                  cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  lrn::k_count_positive<<<lrn::grid_for(n, 256, 152 * 8), 256, 0, s>>>(labels, n, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_count(const unsigned char *labels, long long n, unsigned long long seed,
+                                unsigned long long thr0, unsigned long long thr1, unsigned *block_count,
+                                cudaStream_t s) {
+  lrn::k_sample_pass<false><<<lrn::kSampleBlocks, lrn::kSampleThreads, 0, s>>>(labels, n, seed, thr0, thr1,
+                                                                                block_count, nullptr, 0, nullptr,
+                                                                                nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sample_write(const Geom &g, const double *U, const unsigned char *labels, unsigned long long seed,
+                                unsigned long long thr0, unsigned long long thr1, const long long *offsets,
+                                long long capacity, long long rows, long long *cells, float *x, float *y,
+                                cudaStream_t s) {
+  const long long n = (long long)g.nx * g.ny;
+  lrn::k_sample_pass<true><<<lrn::kSampleBlocks, lrn::kSampleThreads, 0, s>>>(labels, n, seed, thr0, thr1, nullptr,
+                                                                               offsets, capacity, cells, y);
+  if (rows > 0) lrn::k_features_of<<<lrn::grid_for(rows, 128, 152 * 32), 128, 0, s>>>(g, U, cells, rows, x);
   return cudaGetLastError();
 }
 

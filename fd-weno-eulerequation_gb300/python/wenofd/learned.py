@@ -1,29 +1,32 @@
 """Training workflow of the learned troubled-cell indicator.
 
 Data come from the solver itself: shear-layer (or Riemann) runs at seeds other
-than the evaluation seed; at several times, every cell's 50 features and its
-WENO-Z label are extracted on the GPU (wenofd_indicator_data) and a balanced
-sample is kept.  Training runs the project's FP32 forward / backward / Adam
-kernels (wenofd_mlp_train).  torch supplies device buffers only.
+than the evaluation seed; at several times a balanced sample of cells, their
+50 features and WENO-Z labels, is formed on the GPU (wenofd_indicator_sample).
+Training runs the project's FP32 forward / backward / Adam kernels
+(wenofd_mlp_train) from wenofd_mlp_init's parameters.  torch supplies device
+buffers only; the same steps through the C ABI alone are
+fd-weno-eulerequation_gb300/host/train_indicator.cpp, which gives the same
+parameters bit for bit.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from . import FP32, MLP_INPUTS, MLP_PARAMS, Solver, mlp_forward, mlp_train
+from . import FP32, MLP_INPUTS, Solver, mlp_forward, mlp_init, mlp_train
 
 
 def init_params(seed: int) -> np.ndarray:
-    """Uniform He-style initialisation (same layout as the C ABI)."""
-    rng = np.random.default_rng(seed)
-    p = np.zeros(MLP_PARAMS, dtype=np.float32)
-    p[0:1600] = rng.uniform(-1, 1, 1600) * np.sqrt(6.0 / 50)
-    p[1632:2656] = rng.uniform(-1, 1, 1024) * np.sqrt(6.0 / 32)
-    p[2688:2720] = rng.uniform(-1, 1, 32) * np.sqrt(6.0 / 32)
-    return p
+    """Uniform He-style initialisation (wenofd_mlp_init)."""
+    return mlp_init(seed)
 
 
 DEFAULT_RUNS = ((5, 11), (5, 12), (4, 13), (4, 14))
+
+
+def sample_seed_of(sample_seed: int, run: int, snapshot: int) -> int:
+    """Seed of the device sampler for one snapshot of one run."""
+    return (sample_seed * 1_000_003 + run * 1_009 + snapshot) & 0xFFFFFFFFFFFFFFFF
 
 
 def generate_dataset(torch, runs=DEFAULT_RUNS, n: int = 512, snapshots=(40, 120, 240, 400),
@@ -31,42 +34,28 @@ def generate_dataset(torch, runs=DEFAULT_RUNS, n: int = 512, snapshots=(40, 120,
                      label_deviation: float = 1e-2):
     """Features X (N, 50) and labels y (N,) as CUDA float32 tensors: for each
     (testcase, seed) run, an FP32-form solve at n x n, and at each snapshot
-    step a sample of `per_snapshot` cells, half flagged and half not where
-    possible.  Defaults: two shear layers and two seeded Riemann problems,
-    4 x 4 x 125k = 2e6 stencils."""
-    gen = torch.Generator(device=f"cuda:{device}")
-    gen.manual_seed(sample_seed)
-    Xs, ys = [], []
-    cells = n * n
-    feat = torch.empty((cells, MLP_INPUTS), dtype=torch.float32, device=f"cuda:{device}")
-    lab = torch.empty(cells, dtype=torch.uint8, device=f"cuda:{device}")
-    for testcase, seed in runs:
+    step a device-side sample of about `per_snapshot` cells, half flagged and
+    half not where possible (wenofd_indicator_sample), appended in order.
+    Defaults: two shear layers and two seeded Riemann problems, 4 x 4 x 125k
+    = 2e6 stencils."""
+    slack = 1.05
+    cap = int(len(runs) * len(snapshots) * (per_snapshot * slack + 1024))
+    X = torch.empty((cap, MLP_INPUTS), dtype=torch.float32, device=f"cuda:{device}")
+    y = torch.empty(cap, dtype=torch.float32, device=f"cuda:{device}")
+    rows = 0
+    for r, (testcase, seed) in enumerate(runs):
         with Solver({"TESTCASE": testcase, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
                      "SEED": seed, "PRECISION": FP32, "DEVICE": device, "TEND": 1.0e9,
                      "LABEL_DEVIATION": label_deviation}) as s:
             s.initialize()
             done = 0
-            for snap in snapshots:
+            for k, snap in enumerate(snapshots):
                 s.advance(max_steps=snap - done)
                 done = snap
-                s.indicator_data(feat.data_ptr(), lab.data_ptr())
-                torch.cuda.synchronize(device)
-                pos = torch.nonzero(lab, as_tuple=True)[0]
-                neg = torch.nonzero(lab == 0, as_tuple=True)[0]
-                k_pos = min(len(pos), per_snapshot // 2)
-                k_neg = min(len(neg), per_snapshot - k_pos)
-                pick = []
-                if k_pos:
-                    pick.append(pos[torch.randperm(len(pos), generator=gen, device=pos.device)[:k_pos]])
-                if k_neg:
-                    pick.append(neg[torch.randperm(len(neg), generator=gen, device=neg.device)[:k_neg]])
-                idx = torch.cat(pick)
-                Xs.append(feat[idx].clone())
-                ys.append(lab[idx].float())
-    X = torch.cat(Xs)
-    y = torch.cat(ys)
-    perm = torch.randperm(len(y), generator=gen, device=y.device)
-    return X[perm].contiguous(), y[perm].contiguous()
+                rows += s.indicator_sample(per_snapshot, sample_seed_of(sample_seed, r, k), X[rows:].data_ptr(),
+                                           y[rows:].data_ptr(), cap - rows)
+    torch.cuda.synchronize(device)
+    return X[:rows].contiguous(), y[:rows].contiguous()
 
 
 def train(torch, X, y, epochs: int = 20, batch: int = 4096, lr: float = 3e-3, seed: int = 1,

@@ -4,6 +4,7 @@ reference fails on them (before any device work)."""
 import os
 import re
 
+import numpy as np
 import pytest
 
 import wenofd
@@ -70,3 +71,15 @@ def test_config_file_parser_semantics(tmp_path):
     with pytest.raises(wenofd.WenofdError) as e:
         wenofd.Solver(config_file=str(p))
     assert "Invalid example" in str(e.value)
+
+
+def test_mlp_init_is_seeded_and_scaled():
+    """wenofd_mlp_init (host only): the same seed gives the same parameters,
+    weights within their He-uniform ranges, biases zero."""
+    a, b, c = wenofd.mlp_init(7), wenofd.mlp_init(7), wenofd.mlp_init(8)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    w1, b1, w2, b2, w3, b3 = a[:1600], a[1600:1632], a[1632:2656], a[2656:2688], a[2688:2720], a[2720]
+    assert np.abs(w1).max() <= np.sqrt(6 / 50) and np.abs(w1).max() > 0.9 * np.sqrt(6 / 50)
+    assert np.abs(w2).max() <= np.sqrt(6 / 32) and np.abs(w3).max() <= np.sqrt(6 / 32)
+    assert not b1.any() and not b2.any() and b3 == 0.0
+    assert abs(float(w1.mean())) < 0.05
