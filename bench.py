@@ -15,7 +15,8 @@ solver-produced stencils at other seeds.  The FP32 form (WENO-Z everywhere)
 and the plain FP64 WENO-Z path, bitwise equal to the reference, are measured
 in the same run on the same GPU.  L1 density errors are reported against the
 plain FP64 path on the same grid after the same steps, and against a 2x finer
-plain FP64 solution at 513^2 (the accuracy bar: <= 1.5x plain FP64's error).
+plain FP64 solution at 2049^2 (the shear layer at 1025^2, t = 0.1; the
+accuracy bar: <= 1.5x plain FP64's error).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -300,7 +301,7 @@ def train_indicator(torch, device: int):
     return params, info
 
 
-def finer_reference_errors(wenofd, params, device: int, n: int = 513, t_end: float = 0.1) -> dict:
+def finer_reference_errors(wenofd, params, device: int, n: int = 1025, t_end: float = 0.1) -> dict:
     """L1 density error of each form against plain FP64 WENO-Z on the 2x
     finer node grid (2n-1)^2 at the same end time (fine node 2k = coarse node
     k): the shear layer (seed SEED) at n^2, and a seeded four-quadrant Riemann
