@@ -297,33 +297,34 @@ __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ unsigned bf2_bits(__nv_bfloat162 v) { return *reinterpret_cast<unsigned *>(&v); }
 __device__ __forceinline__ __nv_bfloat162 bits_bf2(unsigned u) { return *reinterpret_cast<__nv_bfloat162 *>(&u); }
 
-// GELU (tanh form) of two pre-activations in packed BF16 arithmetic with the
-// hardware tanh: 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))).  The
-// result is the next layer's BF16 operand, so BF16 intermediates lose
-// nothing that the operand rounding keeps.
-__device__ __forceinline__ unsigned gelu_bf16x2(float z0, float z1) {
+// Twice the GELU (tanh form) of two pre-activations in packed BF16
+// arithmetic with the hardware tanh: z (1 + tanh(sqrt(2/pi) (z + 0.044715
+// z^3))).  The factor 1/2 of GELU is folded into the next layer's BF16
+// weights (pack_indicator_weights halves them, exactly), which gives the
+// same MMA products as 0.5 z (1 + t) against unhalved weights and saves one
+// packed multiply per pair.  The result is the next layer's BF16 operand,
+// so BF16 intermediates lose nothing that the operand rounding keeps.
+__device__ __forceinline__ unsigned gelu2_bf16x2(float z0, float z1) {
   const __nv_bfloat162 z = __floats2bfloat162_rn(z0, z1);
   const __nv_bfloat162 k1 = __float2bfloat162_rn(0.7978845608028654f);
   const __nv_bfloat162 k3 = __float2bfloat162_rn(0.7978845608028654f * 0.044715f);
-  const __nv_bfloat162 half = __float2bfloat162_rn(0.5f);
   const __nv_bfloat162 u = __hmul2(z, __hfma2(__hmul2(z, z), k3, k1));
   unsigned t;
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(bf2_bits(u)));
-  const __nv_bfloat162 h = __hmul2(z, half);
-  return bf2_bits(__hfma2(h, bits_bf2(t), h));
+  return bf2_bits(__hfma2(z, bits_bf2(t), z));
 }
 
-// GELU of the 32 accumulator columns of this thread's row into columns
+// 2 x GELU of the 32 accumulator columns of this thread's row into columns
 // 0..31 of A2 [128 x 48], and columns 32..47 = 1, 1, 0, ... (bias inputs).
 __device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row) {
   constexpr int kc = kK2 / 8;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     uint4 q;
-    q.x = gelu_bf16x2(z[8 * c + 0], z[8 * c + 1]);
-    q.y = gelu_bf16x2(z[8 * c + 2], z[8 * c + 3]);
-    q.z = gelu_bf16x2(z[8 * c + 4], z[8 * c + 5]);
-    q.w = gelu_bf16x2(z[8 * c + 6], z[8 * c + 7]);
+    q.x = gelu2_bf16x2(z[8 * c + 0], z[8 * c + 1]);
+    q.y = gelu2_bf16x2(z[8 * c + 2], z[8 * c + 3]);
+    q.z = gelu2_bf16x2(z[8 * c + 4], z[8 * c + 5]);
+    q.w = gelu2_bf16x2(z[8 * c + 6], z[8 * c + 7]);
     *reinterpret_cast<uint4 *>(&A[canon_off(row, 8 * c, kc)]) = q;
   }
   *reinterpret_cast<uint4 *>(&A[canon_off(row, 32, kc)]) = make_uint4(0x3F803F80u, 0u, 0u, 0u);  // two BF16 1.0
@@ -413,8 +414,16 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
   const unsigned mb = smem_u32(&mbar);
   const unsigned lane_base = unsigned(32 * warp) << 16;
   const float gam = float(g.gamma);
+  // Each CTA takes a contiguous run of tiles in strip-major order (a strip =
+  // 32 columns, tiles 4 rows each down it).  The node patch is a ring of 8
+  // rows, node row i in slot i & 7: consecutive tiles of a strip share 4 of
+  // their 8 patch rows, so a tile that follows its neighbour loads 4 rows.
+  const int tiles_i = (g.nx + kTileI - 1) / kTileI;
   const int tiles_j = (g.ny + kTileJ - 1) / kTileJ;
-  const int ntiles = ((g.nx + kTileI - 1) / kTileI) * tiles_j;
+  const long long ntiles = (long long)tiles_i * tiles_j;
+  const long long first = ntiles * blockIdx.x / gridDim.x, last = ntiles * (blockIdx.x + 1) / gridDim.x;
+  static_assert(kPI == 2 * kTileI, "ring of two tiles' rows");
+  int prev_strip = -1, prev_ti = -2;
   unsigned parity = 0;
 
   // One layer: barrier (the operand writes are visible to the tensor core),
@@ -440,20 +449,26 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
     return true;
   };
 
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int i0 = (tile / tiles_j) * kTileI, j0 = (tile % tiles_j) * kTileJ;
-    // 1. node patch: nodes (i0-2 .. i0+5, j0-2 .. j0+33) of the interior index
-    // space; every load of a thread is issued before any is used
+  for (long long t = first; t < last; ++t) {
+    const int strip = int(t / tiles_i), ti = int(t - (long long)strip * tiles_i);
+    const int i0 = ti * kTileI, j0 = strip * kTileJ;
+    const int row0 = (strip == prev_strip && ti == prev_ti + 1) ? kPI - kTileI : 0;  // first patch row to load
+    prev_strip = strip;
+    prev_ti = ti;
+    // 1. node patch rows row0..7: nodes (i0-2+row, j0-2 .. j0+33) of the
+    // interior index space, into ring slot (i0-2+row) & 7; every load of a
+    // thread is issued before any is used
     {
       constexpr int NP = (kPI * kPJ + kCells - 1) / kCells;
+      const int count = (kPI - row0) * kPJ;
       double v[NP][4];
       bool ok[NP];
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const int k = tid + q * kCells;
-        const int pi = k / kPJ, pj = k - (k / kPJ) * kPJ;
+        const int pi = row0 + k / kPJ, pj = k - (k / kPJ) * kPJ;
         const int ei = kGhost + i0 - 2 + pi, ej = kGhost + j0 - 2 + pj;
-        ok[q] = k < kPI * kPJ && ei < g.nxt && ej < g.nyt;
+        ok[q] = k < count && ei < g.nxt && ej < g.nyt;
         const double *src = U + (long long)ei * g.pitch + ej;
 #pragma unroll
         for (int r = 0; r < 4; ++r) v[q][r] = ok[q] ? __ldg(src + r * g.plane) : 0.0;
@@ -461,14 +476,16 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const int k = tid + q * kCells;
-        if (k < kPI * kPJ) {
+        if (k < count) {
+          const int pi = row0 + k / kPJ, pj = k - (k / kPJ) * kPJ;
           float r = 1.0f, p = 1.0f;
           if (ok[q]) {
             r = dev::f64_to_f32(v[q][0]);
             p = pressure32(gam, r, dev::f64_to_f32(v[q][1]), dev::f64_to_f32(v[q][2]), dev::f64_to_f32(v[q][3]));
           }
-          sRho[k] = r;
-          sPre[k] = p;
+          const int slot = ((i0 - 2 + pi) & (kPI - 1)) * kPJ + pj;
+          sRho[slot] = r;
+          sPre[slot] = p;
         }
       }
     }
@@ -476,16 +493,19 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
     // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1
     {
       const int ci = warp, cj = tid & 31;
+      int rows[5];  // ring slots of node rows i0 + ci - 2 .. i0 + ci + 2
+#pragma unroll
+      for (int a = 0; a < 5; ++a) rows[a] = ((i0 + ci - 2 + a) & (kPI - 1)) * kPJ + cj;
       float w[25];
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[(ci + a) * kPJ + cj + b];
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[rows[a] + b];
       window_store(w, sA1, tid, 0, 1.0f, 1.0f);  // columns 25, 26: bias inputs
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[(ci + a) * kPJ + cj + b];
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[rows[a] + b];
       window_store(w, sA1, tid, kColP, 0.0f, 0.0f);
     }
     // 3. layer 1 (bias included)
@@ -558,13 +578,15 @@ void pack_indicator_weights(const float *params, void *host_out) {
     hi_lo(params[oB1 + o], hi, lo);
     put(w->w1, o, kColBias1, kK1 / 8, hi);
     put(w->w1, o, kColBias1 + 1, kK1 / 8, lo);
-    for (int k = 0; k < kHid; ++k) put(w->w2, o, k, kK2 / 8, params[oW2 + o * kHid + k]);
+    // layers 2 and 3 take 2 x GELU (gelu2_bf16x2): their weights on it are
+    // halved here, exactly (a power of two); their bias columns are not
+    for (int k = 0; k < kHid; ++k) put(w->w2, o, k, kK2 / 8, 0.5f * params[oW2 + o * kHid + k]);
     hi_lo(params[oB2 + o], hi, lo);
     put(w->w2, o, kHid, kK2 / 8, hi);
     put(w->w2, o, kHid + 1, kK2 / 8, lo);
     hi_lo(params[oW3 + o], hi, lo);
-    put(w->w3, 0, o, kK2 / 8, hi);
-    put(w->w3, 1, o, kK2 / 8, lo);
+    put(w->w3, 0, o, kK2 / 8, 0.5f * hi);
+    put(w->w3, 1, o, kK2 / 8, 0.5f * lo);
   }
   hi_lo(params[oB3], hi, lo);
   put(w->w3, 0, kHid, kK2 / 8, hi);
