@@ -23,7 +23,7 @@ using wenofd::BatchMemberStatus;
 using wenofd::Ctrl;
 
 struct wenofd_batch {
-  int device = 0, n = 0, precision = 0, scheme = 0;
+  int device = 0, n = 0, precision = 0, scheme = 0, rk = 2;
   std::vector<wenofd_solver *> members;
   cudaStream_t stream = nullptr;
   // work plan (device)
@@ -77,6 +77,7 @@ BatchArgs make_args(const wenofd_batch *b, int nsteps) {
   a.work.pt_prefix = b->d_prefix + 2 * (b->n + 1);
   a.n = b->n;
   a.nsteps = nsteps;
+  a.rk = b->rk;
   a.counters = b->d_counters;
   a.barrier = b->d_barrier;
   a.error = b->d_flags;
@@ -253,10 +254,10 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
     if (!s) return fail(WENOFD_BAD_ARG, "null member handle at index " + std::to_string(m));
     if (s->precision == WENOFD_LEARNED)
       return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + ": the learned form is not batched");
-    if (s->rk != 2) return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + ": batches run RKMETH 2 (SSP-RK3)");
-    if (s->precision != members[0]->precision || s->scheme != members[0]->scheme ||
+    if (s->precision != members[0]->precision || s->scheme != members[0]->scheme || s->rk != members[0]->rk ||
         s->device != members[0]->device)
-      return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + ": PRECISION, SCHEME and DEVICE must match member 0");
+      return fail(WENOFD_BAD_ARG,
+                  "member " + std::to_string(m) + ": PRECISION, SCHEME, RKMETH and DEVICE must match member 0");
     for (int k = 0; k < m; ++k)
       if (members[k] == s) return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + " repeats member " + std::to_string(k));
   }
@@ -265,6 +266,7 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
   b->n = n;
   b->precision = members[0]->precision;
   b->scheme = members[0]->scheme;
+  b->rk = members[0]->rk;
   b->members.assign(members, members + n);
   for (const wenofd_solver *s : b->members) b->cells += (long long)s->nx * s->ny;
   auto bail = [&](int rc) {

@@ -256,8 +256,40 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
     for_member_items(b, cnt + 1, b.work.pt_prefix, sM, exact_pass);
     barrier(finalize);
 
-    // SSP-RK3: S -> A -> B -> S (src/WENOFD.cpp:352-396)
-    for (int st = 0; st < 3; ++st) {
+    // m_now += dt; count++ (src/WENOFD.cpp:213-224), then the next step's
+    // gate; after the launch's last step, the host summary
+    const bool last_step = step == b.nsteps - 1;
+    auto step_end = [&]() {
+      int alive = 0, err = 0;
+      for (int base = 0; base < n; base += NT) {
+        const int m = base + int(threadIdx.x);
+        int can = 0, e = 0;
+        if (m < n) {
+          Ctrl *c = b.members[m].ctrl;
+          if (__ldcg(&c->active)) {
+            const double now = __ldcg(&c->now) + __ldcg(&c->dt);
+            c->now = now;
+            c->steps = __ldcg(&c->steps) + 1;
+            c->done = !(fabs(now - __ldcg(&c->t_end)) > 1e-9);
+          }
+          can = runnable(c);
+          c->active = can;
+          e = __ldcg(&c->error) != 0;
+        }
+        alive += __syncthreads_count(can);
+        err |= __syncthreads_or(e);
+      }
+      if (last_step && threadIdx.x == 0) {
+        b.status[0] = alive;
+        b.status[1] = err;
+      }
+    };
+
+    // The stages of RKMETH (src/WENOFD.cpp:301-396), buffers as the single
+    // solve uses them: SSP-RK3 S -> A -> B -> S; SSP-RK2 S -> A -> S; RK1
+    // S -> A, then A's interior copied to S.
+    const int nst = b.rk + 1;
+    for (int st = 0; st < nst; ++st) {
       for_member_items(b, cnt + 2 + 2 * st, b.work.bc_prefix, sM, [&](int local, const BatchMember &M) {
         double *in = st == 0 ? M.S : (st == 1 ? M.A : M.B);
         const int first = local * kBcChunk, total = bc_entries(M.g);
@@ -270,52 +302,41 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         StageArgs a;
         a.uin = st == 0 ? M.S : (st == 1 ? M.A : M.B);
         a.un = M.S;
-        a.uout = st == 0 ? M.A : (st == 1 ? M.B : M.S);
-        // SSP-RK3 coefficients (src/WENOFD.cpp:369-383)
-        a.a = st == 0 ? 1.0 : (st == 1 ? 3.0 / 4.0 : 1.0 / 3.0);
-        a.b = st == 0 ? 0.0 : (st == 1 ? 1.0 / 4.0 : 2.0 / 3.0);
-        a.c = st == 0 ? 1.0 : (st == 1 ? 1.0 / 4.0 : 2.0 / 3.0);
+        a.uout = st == 0 ? M.A : (st == nst - 1 ? M.S : M.B);
+        if (b.rk == 2) {  // SSP-RK3 (src/WENOFD.cpp:369-383)
+          a.a = st == 0 ? 1.0 : (st == 1 ? 3.0 / 4.0 : 1.0 / 3.0);
+          a.b = st == 0 ? 0.0 : (st == 1 ? 1.0 / 4.0 : 2.0 / 3.0);
+          a.c = st == 0 ? 1.0 : (st == 1 ? 1.0 / 4.0 : 2.0 / 3.0);
+          a.form = st == 0 ? kFormStage1 : (st == 1 ? kFormRK3Mid : kFormGeneric);
+        } else {  // SSP-RK2 (src/WENOFD.cpp:312-350) and RK1 (301-310): (1, 0, 1), then (1/2, 1/2, 1/2)
+          a.a = st == 0 ? 1.0 : 0.5;
+          a.b = st == 0 ? 0.0 : 0.5;
+          a.c = st == 0 ? 1.0 : 0.5;
+          a.form = st == 0 ? kFormStage1 : kFormRK2Mid;
+        }
         a.dt = &M.ctrl->dt;
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
-        a.form = st == 0 ? kFormStage1 : (st == 1 ? kFormRK3Mid : kFormGeneric);
         a.flags = nullptr;
         if constexpr (F32)
           stage_tile_f32<SCHEME, TI, TJ, NT, false, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
         else stage_tile_f64<SCHEME, TI, TJ, NT, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
-      if (st < 2) {
-        barrier(Nothing());
-      } else {
-        // m_now += dt; count++ (src/WENOFD.cpp:213-224), then the next
-        // step's gate; after the launch's last step, the host summary
-        const bool last_step = step == b.nsteps - 1;
-        barrier([&]() {
-          int alive = 0, err = 0;
-          for (int base = 0; base < n; base += NT) {
-            const int m = base + int(threadIdx.x);
-            int can = 0, e = 0;
-            if (m < n) {
-              Ctrl *c = b.members[m].ctrl;
-              if (__ldcg(&c->active)) {
-                const double now = __ldcg(&c->now) + __ldcg(&c->dt);
-                c->now = now;
-                c->steps = __ldcg(&c->steps) + 1;
-                c->done = !(fabs(now - __ldcg(&c->t_end)) > 1e-9);
-              }
-              can = runnable(c);
-              c->active = can;
-              e = __ldcg(&c->error) != 0;
-            }
-            alive += __syncthreads_count(can);
-            err |= __syncthreads_or(e);
-          }
-          if (last_step && threadIdx.x == 0) {
-            b.status[0] = alive;
-            b.status[1] = err;
-          }
-        });
-      }
+      if (st < nst - 1 || b.rk == 0) barrier(Nothing());
+      else barrier(step_end);
+    }
+    if (b.rk == 0) {  // RK1: U^{n+1} = A, interior nodes
+      for_member_items(b, cnt + 4, b.work.pt_prefix, sM, [&](int local, const BatchMember &M) {
+        const long long first = (long long)local * kPtChunk;
+        const long long npts = (long long)M.g.nx * M.g.ny;
+        for (long long t = first + threadIdx.x; t < first + kPtChunk && t < npts; t += NT) {
+          const int i = int(t / M.g.ny), j = int(t - (t / M.g.ny) * M.g.ny);
+          const long long p = (long long)(kGhost + i) * M.g.pitch + (kGhost + j);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) M.S[r * M.g.plane + p] = __ldcg(&M.A[r * M.g.plane + p]);
+        }
+      });
+      barrier(step_end);
     }
   }
 }

@@ -139,7 +139,7 @@ struct BatchWork {
 
 constexpr int kBcChunk = 256;
 constexpr int kPtChunk = 4096;
-constexpr int kBatchPhases = 8;  // work counters per step: dt x 2, (bc, stage) x 3
+constexpr int kBatchPhases = 8;  // work counters per step: dt x 2, (bc, stage) x 3 (RK1: + copy)
 constexpr unsigned kBarrierLimit = 1u << 24;
 // Poll limit of the barrier in the withholding test instance (a few ms).
 constexpr unsigned kBarrierTestLimit = 1u << 12;
@@ -149,6 +149,7 @@ struct BatchArgs {
   BatchWork work;
   int n;               // members
   int nsteps;          // steps per launch
+  int rk;              // RKMETH of every member: 0 RK1, 1 SSP-RK2, 2 SSP-RK3
   unsigned *counters;  // nsteps * kBatchPhases work counters, zeroed before the launch
   unsigned *barrier;   // [0] arrivals (zero before the launch), [1] generation
   int *error;          // set if a barrier wait gave up

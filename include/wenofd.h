@@ -240,9 +240,10 @@ int wenofd_mlp_init(float *host_params, unsigned long long seed);
  * CWENOFD::run (src/WENOFD.cpp:213-224, calculateDeltaT + RunRK3 + m_now += dt)
  * by one kernel launch per few steps that advances every member.
  *
- * Members are existing handles: same device, same SCHEME, RKMETH 2
- * (SSP-RK3) and PRECISION FP64 or FP32 (the learned form is not batched);
- * sizes, test cases, boundary conditions, CFL and TEND may differ.  The
+ * Members are existing handles: same device, same SCHEME, same RKMETH (RK1,
+ * SSP-RK2 or SSP-RK3) and the same PRECISION, FP64 or FP32 (the learned
+ * form is not batched); sizes, test cases, boundary conditions, CFL and TEND
+ * may differ.  The
  * batch works on the members' own device state: a member stepped by a
  * batch is read (wenofd_get_state, wenofd_get_info, ...) through its own
  * handle; members must outlive the batch and must not be advanced through

@@ -90,6 +90,30 @@ def test_fp64_batch_member_matches_oracle():
     assert got[0][1] == p.now
 
 
+@pytest.mark.parametrize("rk", [0, 1], ids=["rk1", "ssprk2"])
+@pytest.mark.parametrize("configure", [None, {"steps_per_launch": 3}], ids=["default", "launch3"])
+def test_rk1_rk2_batches(rk, configure):
+    """RKMETH 0 (RK1: one stage, then U^{n+1} = the stage's output) and 1
+    (SSP-RK2) batches: FP64 members bit for bit the single solves (and the
+    oracle), FP32 members within the FP32 form's bound of their FP64 solve."""
+    cfgs = [dict(_cfg(*m, wenofd.FP64), RKMETH=rk) for m in MEMBERS]
+    steps = 9
+    ref = _alone(cfgs, steps)
+    got, n, _ = _batched(cfgs, steps, configure)
+    assert n == steps
+    for (U, now, k), (Ur, nowr, kr) in zip(got, ref):
+        assert k == kr == steps and now == nowr
+        assert np.array_equal(U, Ur)
+    tc, nx, ny, seed, extra = MEMBERS[0]
+    p = orc.Problem(tc, nx, ny, orc.WENOZ, rk, 0.6, seed=seed)
+    p.run(max_steps=steps)
+    assert np.array_equal(got[0][0], p.interior())
+    got32, _, _ = _batched([dict(c, PRECISION=wenofd.FP32) for c in cfgs], steps, configure)
+    for (U32, _, k), (U64, _, _) in zip(got32, ref):
+        assert k == steps
+        assert np.max(np.abs(U32 - U64)) <= FP32_REL_TOL * np.max(np.abs(U64))
+
+
 @pytest.mark.parametrize("scheme", [orc.WENOJS, orc.WENOZP, orc.WENOZPI])
 def test_fp64_batch_other_schemes(scheme):
     cfgs = [_cfg(*m, wenofd.FP64, scheme=scheme) for m in MEMBERS[:4]]
