@@ -243,7 +243,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   constexpr int kMaxFaces = S::kFace;
   __shared__ __align__(128) unsigned char sflag[ROUTE ? FI * FS : 1];
   __shared__ short slist[ROUTE ? kMaxFaces : 1];
-  __shared__ int scount;
+  __shared__ int scount_x, scount_y;  // WENO faces listed in the x and y sweeps
   __shared__ __align__(8) unsigned long long tma_bar;
   if constexpr (TMA) {
     // The halo box (and the flag box) by TMA, one thread issuing both.
@@ -316,7 +316,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       }
     }
     if constexpr (ROUTE) {
-      if (threadIdx.x == 0) scount = 0;
+      if (threadIdx.x == 0) scount_x = scount_y = 0;
     }
   } else {
   // --- state tile with halo: node (hi, hj) = global (1 + i0 + hi, 1 + j0 + hj).
@@ -395,7 +395,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
           }
         }
       }
-      if (threadIdx.x == 0) scount = 0;
+      if (threadIdx.x == 0) scount_x = scount_y = 0;
     }
   }
   }  // TMA
@@ -414,25 +414,29 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if constexpr (ROUTE) {
       Hf[t] = linear_face4(Fp + t, Fm + t + TJ, TJ);
       const unsigned char *fl = sflag + f * FS + (j + 2 + FO);  // nodes f-2 .. f+1
-      if (fl[0] | fl[FS] | fl[2 * FS] | fl[3 * FS]) slist[atomicAdd(&scount, 1)] = short(t);
+      if (fl[0] | fl[FS] | fl[2 * FS] | fl[3 * FS]) slist[atomicAdd(&scount_x, 1)] = short(t);
     } else {
       Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
                                     Fm + t + TJ, TJ);
     }
   }
+  // The listed faces (if any) are recomputed with WENO after the barrier;
+  // with none listed (block-uniform) the second barrier is not needed.
+  __syncthreads();
   if constexpr (ROUTE) {
-    __syncthreads();
-    const int nw = scount;
-    for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {  // 4 lanes per face, whole warps
-      const int q4 = base + (threadIdx.x & 31);
-      const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
-      const int f = t / TJ, j = t - (t / TJ) * TJ;
-      const float o = weno_face_lane<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3],
-                                                Fp + t, Fm + t + TJ, TJ, q4 & 3);
-      if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+    const int nw = scount_x;
+    if (nw) {
+      for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {  // 4 lanes per face, whole warps
+        const int q4 = base + (threadIdx.x & 31);
+        const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
+        const int f = t / TJ, j = t - (t / TJ) * TJ;
+        const float o = weno_face_lane<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3],
+                                                  Fp + t, Fm + t + TJ, TJ, q4 & 3);
+        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
 
   // x term of the node's RHS (rhs zeroed, then += in the x sweep)
   constexpr int PPT = (TI * TJ + NT - 1) / NT;
@@ -447,10 +451,9 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       rhs[k] = join2(__fmul2_rn(sub2(lo2(hr), lo2(hl)), mi), __fmul2_rn(sub2(hi2(hr), hi2(hl)), mi));
     }
   }
-  if constexpr (ROUTE) {
-    if (threadIdx.x == 0) scount = 0;
-  }
-  __syncthreads();
+  // No barrier here: the y split writes only Fp and Fm, whose readers (the x
+  // faces and the x list) are behind the barriers above; Hf, which the x term
+  // reads, is rewritten only after the next barrier.
 
   // --- y sweep: split fluxes of tile rows, halo columns 0..HJ-1
   for (int t = threadIdx.x; t < TI * HJ; t += NT) {
@@ -466,26 +469,28 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if constexpr (ROUTE) {
       Hf[t] = linear_face4(Fp + s, Fm + s + 1, 1);
       const unsigned char *fl = sflag + (i + 2) * FS + f + FO;  // nodes f-2 .. f+1 along y
-      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount, 1)] = short(t);
+      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount_y, 1)] = short(t);
     } else {
       Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,
                                     Fm + s + 1, 1);
     }
   }
+  __syncthreads();
   if constexpr (ROUTE) {
-    __syncthreads();
-    const int nw = scount;
-    for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {
-      const int q4 = base + (threadIdx.x & 31);
-      const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
-      const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
-      const int s = i * HJ + f;
-      const float o = weno_face_lane<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3],
-                                                Fp + s, Fm + s + 1, 1, q4 & 3);
-      if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+    const int nw = scount_y;
+    if (nw) {
+      for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {
+        const int q4 = base + (threadIdx.x & 31);
+        const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
+        const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
+        const int s = i * HJ + f;
+        const float o = weno_face_lane<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3],
+                                                  Fp + s, Fm + s + 1, 1, q4 & 3);
+        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
 
   // --- y term, source, RK combination in FP64, store
   const double dt = COH ? __ldcg(a.dt) : *a.dt;
