@@ -414,16 +414,19 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
   const unsigned mb = smem_u32(&mbar);
   const unsigned lane_base = unsigned(32 * warp) << 16;
   const float gam = float(g.gamma);
-  // Each CTA takes a contiguous run of tiles in strip-major order (a strip =
-  // 32 columns, tiles 4 rows each down it).  The node patch is a ring of 8
-  // rows, node row i in slot i & 7: consecutive tiles of a strip share 4 of
-  // their 8 patch rows, so a tile that follows its neighbour loads 4 rows.
+  // CTA b walks one band of rows down one strip (a strip = 32 columns, tiles
+  // of 4 rows each): strip b % tiles_j, band b / tiles_j of the grid's
+  // gridDim.x / tiles_j bands.  CTAs of neighbouring strips and the same band
+  // start at the same row and move down together, so the patch columns they
+  // share are read from L2 while both need them.  The node patch is a ring
+  // of 8 rows, node row i in slot i & 7: consecutive tiles of a strip share 4
+  // of their 8 patch rows, so every tile after a band's first loads 4 rows.
   const int tiles_i = (g.nx + kTileI - 1) / kTileI;
   const int tiles_j = (g.ny + kTileJ - 1) / kTileJ;
-  const long long ntiles = (long long)tiles_i * tiles_j;
-  const long long first = ntiles * blockIdx.x / gridDim.x, last = ntiles * (blockIdx.x + 1) / gridDim.x;
+  const int bands = int(gridDim.x) / tiles_j;
+  const int strip = int(blockIdx.x) % tiles_j, band = int(blockIdx.x) / tiles_j;
+  const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
   static_assert(kPI == 2 * kTileI, "ring of two tiles' rows");
-  int prev_strip = -1, prev_ti = -2;
   unsigned parity = 0;
 
   // One layer: barrier (the operand writes are visible to the tensor core),
@@ -449,12 +452,9 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
     return true;
   };
 
-  for (long long t = first; t < last; ++t) {
-    const int strip = int(t / tiles_i), ti = int(t - (long long)strip * tiles_i);
+  for (int ti = first; ti < last; ++ti) {
     const int i0 = ti * kTileI, j0 = strip * kTileJ;
-    const int row0 = (strip == prev_strip && ti == prev_ti + 1) ? kPI - kTileI : 0;  // first patch row to load
-    prev_strip = strip;
-    prev_ti = ti;
+    const int row0 = ti > first ? kPI - kTileI : 0;  // first patch row to load
     // 1. node patch rows row0..7: nodes (i0-2+row, j0-2 .. j0+33) of the
     // interior index space, into ring slot (i0-2+row) & 7; every load of a
     // thread is issued before any is used
@@ -596,18 +596,19 @@ void pack_indicator_weights(const float *params, void *host_out) {
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
                              unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
                              cudaStream_t s) {
-  const int tiles = ((g.nx + lrn::kTileI - 1) / lrn::kTileI) * ((g.ny + lrn::kTileJ - 1) / lrn::kTileJ);
-  // persistent CTAs: as many as are resident at once (tiles are dealt round
-  // robin, so a second wave would double the time): kResident per SM, the
-  // kernel's launch bound, which its shared memory, registers and tensor
-  // memory meet
+  const int tiles_i = (g.nx + lrn::kTileI - 1) / lrn::kTileI, tiles_j = (g.ny + lrn::kTileJ - 1) / lrn::kTileJ;
+  // CTAs: one per (strip, band of rows); as many bands as let every CTA be
+  // resident at once (kResident per SM, the kernel's launch bound, which its
+  // shared memory, registers and tensor memory meet), at least one
   static int sms_of[64] = {0};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   int &sms = sms_of[dev & 63];
   if (sms == 0 && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  const int grid = tiles < sms * lrn::kResident ? tiles : sms * lrn::kResident;
+  int bands = (sms * lrn::kResident) / tiles_j;
+  bands = bands < 1 ? 1 : (bands > tiles_i ? tiles_i : bands);
+  const int grid = tiles_j * bands;
   lrn::k_indicator_tc<<<grid, lrn::kCells, 0, s>>>(g, U, static_cast<const lrn::IndicatorWeights *>(weights),
                                                    logit_threshold, flags, g.pitch, error, active, ctrl,
                                                    interval);

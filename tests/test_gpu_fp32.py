@@ -124,3 +124,46 @@ def test_fused_screen_steps_equal_separate_steps(precision, tile_i):
         Ub = b.get_state()
     assert ta == now
     assert np.array_equal(Ua, Ub)
+
+
+@pytest.mark.parametrize("nx,ny", [(6, 6), (7, 9), (16, 31), (33, 65), (100, 7)])
+@pytest.mark.parametrize("tile_i", [15, 31])
+def test_tma_tiles_on_small_and_ragged_grids(nx, ny, tile_i):
+    """The per-solve FP32 tiles take their halo and flags by TMA in boxes of
+    40 x (TI + 6) nodes and 48 x (TI + 4) flag bytes: on grids smaller than a
+    box or not a multiple of the tile the boxes run past the arrays (zero
+    fill) and past the tiles' last nodes.  The batched kernel runs the same
+    tile arithmetic with per-thread 128-bit loads instead, so the two must
+    agree (to the last bit here), on every boundary kind.  On the smallest
+    Riemann grids a shock crosses most nodes and FP32 rounding grows: the FP32
+    form sits up to ~3e-4 from FP64 there, and the learned form with every
+    node flagged (the WENO list for every face, whose four lanes group the
+    arithmetic differently) up to ~2e-4 from the FP32 form; both are held to
+    1e-3."""
+    for tc in (orc.RIEMANN_SEEDED, orc.RIEMANN1, orc.SMOOTH):
+        cfg = {"TESTCASE": tc, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "SEED": 4}
+
+        def run(precision, params=None, batched=False):
+            with wenofd.Solver(dict(cfg, PRECISION=precision, TILE_I=tile_i)) as s:
+                s.initialize()
+                if params is not None:
+                    s.set_indicator(params, 0.5)
+                if batched:
+                    with wenofd.Batch([s]) as b:
+                        b.configure(tile_i=tile_i)
+                        assert b.advance(5) == 5
+                else:
+                    assert s.advance(max_steps=5) == 5
+                return s.get_state()
+
+        U64 = run(wenofd.FP64) if tile_i == 15 else None
+        U32 = run(wenofd.FP32)
+        scale = np.max(np.abs(U32))
+        assert np.all(np.isfinite(U32))
+        assert np.max(np.abs(U32 - run(wenofd.FP32, batched=True))) <= 1e-12 * scale, (tc, nx, ny)
+        every = np.zeros(wenofd.MLP_PARAMS, dtype=np.float32)
+        every[2720] = 50.0
+        Ul = run(wenofd.LEARNED, every)
+        if U64 is not None:
+            assert np.max(np.abs(U32 - U64)) <= 1e-3 * scale, (tc, nx, ny)
+        assert np.max(np.abs(Ul - U32)) <= 1e-3 * scale, (tc, nx, ny)
