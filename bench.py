@@ -45,11 +45,13 @@ SEED = 2024
 # --indicator-interval): probability above which a node is flagged, the WENO-Z
 # weight deviation that labels a training node (1e-2, the learned form's
 # specification), and the time steps per indicator run.  Chosen from sweeps:
-# L1 error vs the 2x finer FP64 reference within 3 % of plain FP64 on both
-# reference problems; intervals 2 and 3 leave both errors unchanged.
+# L1 error vs the 2x finer FP64 reference within 4 % of plain FP64 on both
+# reference problems; intervals 2 to 5 leave both errors unchanged to within a
+# few tenths of a percent (at CFL 0.7 a front moves under one node per step,
+# and a face takes WENO within two nodes of a flagged node).
 THRESHOLD = 0.8
 LABEL_DEVIATION = 1e-2
-INDICATOR_INTERVAL = 3  # time steps per indicator run (--indicator-interval)
+INDICATOR_INTERVAL = 4  # time steps per indicator run (--indicator-interval)
 # Training is repeatable bit for bit; of training seeds 1-8 this one gave the
 # lowest binary cross-entropy on held-out stencils (solver runs at seeds used
 # neither for training nor for the workload).

@@ -199,7 +199,7 @@ def test_learned_error_on_the_shear_layer_at_1025():
     (seed 2024) at 1025^2 to t = 0.1, learned + FP32 (trained as the bench
     trains: two shear layers and two Riemann problems at other seeds, labels
     at WENO-Z weight deviation 1e-2, seed 7; threshold 0.8, indicator every
-    third step) against a plain FP64 WENO-Z solution on the 2x finer 2049^2
+    fourth step) against a plain FP64 WENO-Z solution on the 2x finer 2049^2
     grid (fine node 2k = coarse node k); its L1 density error is at most 1.5x
     that of plain FP64 at 1025^2."""
     X, y = learned.generate_dataset(torch, label_deviation=1e-2)
@@ -208,7 +208,7 @@ def test_learned_error_on_the_shear_layer_at_1025():
 
     def state_at(n, prec, par=None):
         with wenofd.Solver({"TESTCASE": 5, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
-                            "SEED": 2024, "PRECISION": prec, "TEND": 0.1, "INDICATOR_INTERVAL": 3}) as s:
+                            "SEED": 2024, "PRECISION": prec, "TEND": 0.1, "INDICATOR_INTERVAL": 4}) as s:
             s.initialize()
             if par is not None:
                 s.set_indicator(par, 0.8)
