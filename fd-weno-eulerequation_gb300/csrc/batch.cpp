@@ -15,6 +15,7 @@
 
 #include "../../include/wenofd.h"
 #include "solver.h"
+#include "trace.h"
 #include "wenofd_internal.h"
 
 using wenofd::BatchArgs;
@@ -246,6 +247,7 @@ void release(wenofd_batch *b) {
 extern "C" {
 
 int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out) {
+  WENOFD_TRACE("wenofd_batch_create");
   if (!out) return fail(WENOFD_BAD_ARG, "null output pointer");
   *out = nullptr;
   if (!members || n < 1) return fail(WENOFD_BAD_ARG, "a batch needs at least one member");
@@ -322,6 +324,7 @@ int wenofd_batch_get_info(const wenofd_batch *b, wenofd_batch_info *info) {
 }
 
 int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_done) {
+  WENOFD_TRACE("wenofd_batch_advance");
   if (!b) return fail(WENOFD_BAD_ARG, "null batch handle");
   BATCH_TRY(cudaSetDevice(b->device));
   if (int rc = sync_members(b)) return rc;
@@ -394,6 +397,7 @@ int wenofd_batch_test_withhold(wenofd_batch *b, int block, int barrier) {
 }
 
 int wenofd_batch_autotune(wenofd_batch *b, int steps, double *ms_per_step) {
+  WENOFD_TRACE("wenofd_batch_autotune");
   if (!b) return fail(WENOFD_BAD_ARG, "null batch handle");
   if (steps < 1 || steps > 4096) return fail(WENOFD_BAD_ARG, "steps must be in [1, 4096]");
   BATCH_TRY(cudaSetDevice(b->device));

@@ -21,6 +21,7 @@
 
 #include "cases.h"
 #include "solver.h"
+#include "trace.h"
 #include "wenofd_internal.h"
 
 using wenofd::Ctrl;
@@ -417,6 +418,7 @@ const char *wenofd_last_error(void) { return g_error.c_str(); }
 const char *wenofd_version(void) { return "wenofd-gb300 0.1 (sm_103a)"; }
 
 int wenofd_create(const char *const *keys, const char *const *values, int n, wenofd_solver **out) {
+  WENOFD_TRACE("wenofd_create");
   if (n < 0 || (n > 0 && (!keys || !values))) return fail(WENOFD_BAD_ARG, "bad key/value arrays");
   std::map<std::string, std::string> opt;
   for (int i = 0; i < n; ++i) {
@@ -483,6 +485,7 @@ int wenofd_get_info(const wenofd_solver *s, wenofd_info *info) {
 }
 
 int wenofd_initialize(wenofd_solver *s) {
+  WENOFD_TRACE("wenofd_initialize");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   std::vector<double> host(size_t(4) * s->nx * s->ny);
@@ -497,6 +500,7 @@ int wenofd_initialize(wenofd_solver *s) {
 }
 
 int wenofd_set_state(wenofd_solver *s, const double *host_state) {
+  WENOFD_TRACE("wenofd_set_state");
   if (int rc = check_handle(s)) return rc;
   if (!host_state) return fail(WENOFD_BAD_ARG, "null state");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -505,6 +509,7 @@ int wenofd_set_state(wenofd_solver *s, const double *host_state) {
 }
 
 int wenofd_get_state(wenofd_solver *s, double *host_state) {
+  WENOFD_TRACE("wenofd_get_state");
   if (int rc = check_handle(s)) return rc;
   if (!host_state) return fail(WENOFD_BAD_ARG, "null state");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -562,6 +567,7 @@ int wenofd_fill_boundary(wenofd_solver *s) {
 }
 
 int wenofd_get_flux(wenofd_solver *s, double *host_rhs) {
+  WENOFD_TRACE("wenofd_get_flux");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
@@ -573,6 +579,7 @@ int wenofd_get_flux(wenofd_solver *s, double *host_rhs) {
 }
 
 int wenofd_calc_dt(wenofd_solver *s, double *dt) {
+  WENOFD_TRACE("wenofd_calc_dt");
   if (int rc = check_handle(s)) return rc;
   if (!dt) return fail(WENOFD_BAD_ARG, "null dt");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -587,6 +594,7 @@ int wenofd_calc_dt(wenofd_solver *s, double *dt) {
 }
 
 int wenofd_rk_step(wenofd_solver *s, double dt) {
+  WENOFD_TRACE("wenofd_rk_step");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_set_dt(s->ctrl, dt, s->stream));
@@ -596,6 +604,7 @@ int wenofd_rk_step(wenofd_solver *s, double dt) {
 }
 
 int wenofd_step(wenofd_solver *s, double *dt_out) {
+  WENOFD_TRACE("wenofd_step");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
@@ -653,6 +662,7 @@ void drop_graphs(wenofd_solver *s) {
 }  // namespace
 
 int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done) {
+  WENOFD_TRACE("wenofd_advance");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   if (int rc = read_ctrl(s)) return rc;
@@ -704,6 +714,7 @@ int wenofd_advance(wenofd_solver *s, long long max_steps, long long *steps_done)
 }
 
 int wenofd_error_norms(wenofd_solver *s, double out[3]) {
+  WENOFD_TRACE("wenofd_error_norms");
   if (int rc = check_handle(s)) return rc;
   if (!out) return fail(WENOFD_BAD_ARG, "null output");
   if (!s->cs.exact) return fail(WENOFD_NO_EXACT, "this case has no exact solution");
@@ -718,6 +729,7 @@ int wenofd_error_norms(wenofd_solver *s, double out[3]) {
 }
 
 int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
+  WENOFD_TRACE("wenofd_time_stages");
   if (int rc = check_handle(s)) return rc;
   if (!ms_per_launch || reps < 1) return fail(WENOFD_BAD_ARG, "bad arguments");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -787,6 +799,7 @@ int wenofd_routing_flags(wenofd_solver *s, unsigned char *host_flags) {
 }
 
 int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
+  WENOFD_TRACE("wenofd_indicator_flags");
   if (int rc = check_handle(s)) return rc;
   if (!host_flags) return fail(WENOFD_BAD_ARG, "null flags");
   if (s->precision != WENOFD_LEARNED || !s->ind_ready)
@@ -807,6 +820,7 @@ int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
 }
 
 int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *dev_labels) {
+  WENOFD_TRACE("wenofd_indicator_data");
   if (int rc = check_handle(s)) return rc;
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
@@ -816,6 +830,7 @@ int wenofd_indicator_data(wenofd_solver *s, float *dev_features, unsigned char *
 }
 
 int wenofd_output_variables(wenofd_solver *s, double *host_out) {
+  WENOFD_TRACE("wenofd_output_variables");
   if (int rc = check_handle(s)) return rc;
   if (!host_out) return fail(WENOFD_BAD_ARG, "null output");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -855,6 +870,7 @@ int set_clock(wenofd_solver *s, double now, long long steps) {
 }  // namespace
 
 int wenofd_save_state(wenofd_solver *s, const char *path) {
+  WENOFD_TRACE("wenofd_save_state");
   if (int rc = check_handle(s)) return rc;
   if (!path) return fail(WENOFD_BAD_ARG, "null path");
   CUDA_TRY(cudaSetDevice(s->device));
@@ -887,6 +903,7 @@ int wenofd_save_state(wenofd_solver *s, const char *path) {
 }
 
 int wenofd_load_state(wenofd_solver *s, const char *path) {
+  WENOFD_TRACE("wenofd_load_state");
   if (int rc = check_handle(s)) return rc;
   if (!path) return fail(WENOFD_BAD_ARG, "null path");
   FILE *f = std::fopen(path, "rb");
@@ -914,6 +931,7 @@ int wenofd_load_state(wenofd_solver *s, const char *path) {
 
 int wenofd_indicator_sample(wenofd_solver *s, long long per_snapshot, unsigned long long seed, float *dev_x,
                             float *dev_y, long long capacity, long long *rows_out) {
+  WENOFD_TRACE("wenofd_indicator_sample");
   if (int rc = check_handle(s)) return rc;
   if (!dev_x || !dev_y || !rows_out) return fail(WENOFD_BAD_ARG, "null output");
   if (per_snapshot < 2 || capacity < 0) return fail(WENOFD_BAD_ARG, "per_snapshot must be >= 2, capacity >= 0");
@@ -973,6 +991,7 @@ int wenofd_indicator_sample(wenofd_solver *s, long long per_snapshot, unsigned l
 }
 
 int wenofd_conservation_sums(wenofd_solver *s, double out[4]) {
+  WENOFD_TRACE("wenofd_conservation_sums");
   if (int rc = check_handle(s)) return rc;
   if (!out) return fail(WENOFD_BAD_ARG, "null output");
   CUDA_TRY(cudaSetDevice(s->device));

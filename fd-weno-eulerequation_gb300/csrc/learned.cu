@@ -19,6 +19,7 @@
 #include "../../include/wenofd.h"
 
 #include "learned_common.cuh"
+#include "trace.h"
 
 namespace wenofd {
 namespace lrn {
@@ -708,6 +709,7 @@ extern "C" int wenofd_mlp_adam(float *dev_params, const float *dev_grad, float *
 // data and seed give the same parameters bit for bit.
 extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const float *dev_y, long long n, int epochs,
                                 int batch, float lr, unsigned long long seed, float *host_epoch_loss, void *stream) {
+  WENOFD_TRACE("wenofd_mlp_train");
   using namespace wenofd::lrn;
   if (!dev_params || !dev_x || !dev_y || n <= 0 || epochs < 1 || batch < 1) return WENOFD_BAD_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
