@@ -4,13 +4,15 @@
 #pragma once
 
 #include "convert.cuh"
+#include "guard.cuh"
 #include "wenofd_internal.h"
 
 namespace wenofd {
 namespace dev {
 
 __device__ __forceinline__ long long at(const Geom &g, int r, int ei, int ej) {
-  return r * g.plane + (long long)ei * g.pitch + ej;
+  return WENOFD_IXC(g.guard, unsigned(r) < 4u && unsigned(ei) < unsigned(g.nxt) && unsigned(ej) < unsigned(g.pitch),
+                    r * g.plane + (long long)ei * g.pitch + ej, 4 * g.plane);
 }
 
 // exchangeGhostCellsValue (src/WENOFD.cpp:850-929, one rank) + setBoundary
@@ -50,7 +52,7 @@ __device__ __forceinline__ void bc_fill_entry(const Geom &g, double *U, const do
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         double v;
-        if (bc == kSpecial) v = special[8 * g.nxt + (side * 4 + r) * g.nyt + ej];
+        if (bc == kSpecial) v = special[WENOFD_SPECIAL(g, 8 * g.nxt + (side * 4 + r) * g.nyt + ej)];
         else v = __ldcg(&U[at(g, r, src, ej)]);
         if (bc == kSlip && r == 1) v *= -1;
         U[at(g, r, dst, ej)] = v;
@@ -67,12 +69,12 @@ __device__ __forceinline__ void bc_fill_entry(const Geom &g, double *U, const do
       for (int r = 0; r < 4; ++r) {
         double v;
         if (bcx == kSpecial) {
-          v = special[8 * g.nxt + (sidex * 4 + r) * g.nyt + ej];
+          v = special[WENOFD_SPECIAL(g, 8 * g.nxt + (sidex * 4 + r) * g.nyt + ej)];
         } else {
           const int col = bcx == kPeriod ? (sidex == 0 ? ex - 1 - kx : sx + kx) : (sidex == 0 ? sx + kx : ex - 1 - kx);
           // y rule at ghost column ei (x periodic: its interior rows hold
           // column col) or at interior column col (x not periodic)
-          if (g.bc_y == kSpecial) v = special[(sidey * 4 + r) * g.nxt + (bcx == kPeriod ? ei : col)];
+          if (g.bc_y == kSpecial) v = special[WENOFD_SPECIAL(g, (sidey * 4 + r) * g.nxt + (bcx == kPeriod ? ei : col))];
           else v = __ldcg(&U[at(g, r, col, srcy)]);
           if (g.bc_y == kSlip && r == 2) v *= -1;
           if (bcx == kSlip && r == 1) v *= -1;
@@ -91,7 +93,7 @@ __device__ __forceinline__ void bc_fill_entry(const Geom &g, double *U, const do
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         double v;
-        if (bc == kSpecial) v = special[(side * 4 + r) * g.nxt + ei];
+        if (bc == kSpecial) v = special[WENOFD_SPECIAL(g, (side * 4 + r) * g.nxt + ei)];
         else v = __ldcg(&U[at(g, r, ei, src)]);
         if (bc == kSlip && r == 2) v *= -1;
         U[at(g, r, ei, dst)] = v;

@@ -5,6 +5,8 @@
 
 #include <math.h>
 
+#include <mutex>
+
 namespace wenofd {
 
 namespace {
@@ -36,7 +38,7 @@ __global__ void k_dt_reduce(Geom g, const double *U, Ctrl *c) {
   dev::SpeedMemo memo;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
-    const long long base = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const long long base = WENOFD_NODE(g, i, j);
     const double rho = U[base], mu = U[g.plane + base], mv = U[2 * g.plane + base], E = U[3 * g.plane + base];
     if (memo.repeat(rho, mu, mv, E)) continue;
     const double u = mu / rho, v = mv / rho;
@@ -80,7 +82,7 @@ __global__ void k_dt_screen(Geom g, const double *U, Ctrl *c) {
   float lo = 0.0f;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
-    const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const long long b = WENOFD_NODE(g, i, j);
     float s, e;
     dev::screen_speed(g, U[b], U[g.plane + b], U[2 * g.plane + b], U[3 * g.plane + b], s, e);
     lo = fmaxf(lo, s - e);
@@ -107,7 +109,7 @@ __global__ void k_dt_refine(Geom g, const double *U, Ctrl *c, const float2 *boun
   int nan_seen = 0;
   dev::SpeedMemo memo;
   auto visit = [&](int i, int j) {
-    const long long b = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const long long b = WENOFD_NODE(g, i, j);
     const double rho = U[b], mu = U[g.plane + b], mv = U[2 * g.plane + b], E = U[3 * g.plane + b];
     float s32, e;
     dev::screen_speed(g, rho, mu, mv, E, s32, e);
@@ -122,7 +124,8 @@ __global__ void k_dt_refine(Geom g, const double *U, Ctrl *c, const float2 *boun
     const int lane = threadIdx.x & 31;
     const int warps = int(gridDim.x * blockDim.x) >> 5;
     for (int t = int(blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += warps) {
-      if (bounds[t].y < L) continue;  // warp-uniform
+      // (bounds are allocated for tiles of 15 rows, the most tiles)
+      if (bounds[WENOFD_IX(g.guard, t, ((g.nx + 14) / 15) * tiles_j)].y < L) continue;  // warp-uniform
       const int i0 = (t / tiles_j) * tile_i, j = (t - (t / tiles_j) * tiles_j) * 32 + lane;
       const int i1 = i0 + tile_i < g.nx ? i0 + tile_i : g.nx;
       if (j < g.ny)
@@ -257,7 +260,7 @@ __global__ void k_output_vars(Geom g, const double *U, double *out03, double *ou
   const long long n = (long long)g.nx * g.ny;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = int(t / g.ny), j = int(t - (t / g.ny) * g.ny);
-    const long long k = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const long long k = WENOFD_NODE(g, i, j);
     const double rho = U[k];
     const double u = U[g.plane + k] / U[k];
     const double v = U[2 * g.plane + k] / U[k];
@@ -281,7 +284,7 @@ __global__ void k_reduce_blocks(Geom g, const double *U, int kind, double t, dou
   const double gy = yl - g.dy * kGhost;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const int i = int(p / g.ny), j = int(p - (p / g.ny) * g.ny);
-    const long long base = (long long)(kGhost + i) * g.pitch + (kGhost + j);
+    const long long base = WENOFD_NODE(g, i, j);
     if (kind == 0) {
       const double x = gx + (kGhost + i) * g.dx, y = gy + (kGhost + j) * g.dy;
       const double uref = 1 + 0.2 * sin(M_PI * (x + y - t));
@@ -309,7 +312,7 @@ __global__ void k_reduce_blocks(Geom g, const double *U, int kind, double t, dou
     }
     __syncthreads();
   }
-  if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x < 4) partials[WENOFD_IX(g.guard, blockIdx.x * 4 + threadIdx.x, 4 * kReduceBlocks)] = sh[threadIdx.x][0];
 }
 
 __global__ void k_reduce_final(Geom g, int kind, const double *partials, int nblk, double *out) {
@@ -328,6 +331,15 @@ __global__ void k_reduce_final(Geom g, int kind, const double *partials, int nbl
   } else {
     for (int q = 0; q < 4; ++q) out[q] = acc[q];
   }
+}
+
+// One index one past the end of buf[4] through the always-on guard (not the
+// macro, so the access is guarded in either build): the guard sends it to
+// buf[0] and records the violation in rec.
+constexpr unsigned long long kSelftestSite = guard_site(__FILE__, __LINE__);
+__global__ void k_guard_selftest(unsigned long long *rec, int *buf) {
+  const int i = dev::guard_ix<kSelftestSite>(rec, true, 4, 4);
+  buf[i] += 1;
 }
 
 int grid_for(long long work, int threads) {
@@ -359,8 +371,37 @@ Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lam
   g.zpl32 = float(zp_lambda);
   g.inv_dx32 = float(1.0 / dx);
   g.inv_dy32 = float(1.0 / dy);
+  g.guard = guard_record();
   return g;
 }
+
+cudaError_t launch_guard_selftest(unsigned long long *rec, int *buf, unsigned long long *site, cudaStream_t s) {
+  k_guard_selftest<<<1, 1, 0, s>>>(rec, buf);
+  *site = kSelftestSite;
+  return cudaGetLastError();
+}
+
+#ifdef WENOFD_BOUNDS_CHECK
+unsigned long long *guard_record() {
+  static std::mutex mu;
+  static unsigned long long *rec[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (rec[dev] == nullptr) {
+    unsigned long long *p = nullptr;
+    if (cudaMalloc(&p, kGuardWords * sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+    if (cudaMemset(p, 0, kGuardWords * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaFree(p);
+      return nullptr;
+    }
+    rec[dev] = p;
+  }
+  return rec[dev];
+}
+#else
+unsigned long long *guard_record() { return nullptr; }
+#endif
 
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s) {
   const long long work = dev::bc_entries(g);

@@ -83,6 +83,7 @@ BatchArgs make_args(const wenofd_batch *b, int nsteps) {
   a.barrier = b->d_barrier;
   a.error = b->d_flags;
   a.status = b->d_flags + 1;
+  a.guard = wenofd::guard_record();
   return a;
 }
 

@@ -111,7 +111,7 @@ __device__ __forceinline__ void for_member_items(const BatchArgs &b, unsigned *c
   auto resolve = [&](int slot, int item) {  // thread 0
     s_item[slot] = item;
     if (item < total) {
-      const int m = owner(prefix, n, item);
+      const int m = WENOFD_IX(b.guard, owner(prefix, n, item), n);
       s_m[slot] = m;
       s_on[slot] = __ldcg(&b.members[m].ctrl->active);
     }
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
     // time-step reduction over each member's interior nodes
     auto node = [&](const BatchMember &M, long long t, double &rho, double &mu, double &mv, double &E) {
       const int i = int(t / M.g.ny), j = int(t - (t / M.g.ny) * M.g.ny);
-      const long long p = (long long)(kGhost + i) * M.g.pitch + (kGhost + j);
+      const long long p = WENOFD_NODE(M.g, i, j);
       rho = __ldcg(&M.S[p]);
       mu = __ldcg(&M.S[M.g.plane + p]);
       mv = __ldcg(&M.S[2 * M.g.plane + p]);
@@ -298,7 +298,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
       });
       barrier(Nothing());
       for_member_items(b, cnt + 3 + 2 * st, b.work.tile_prefix, sM, [&](int local, const BatchMember &M) {
-        const int ti = local / M.tiles_j, tj = local - (local / M.tiles_j) * M.tiles_j;
+        const int ti = WENOFD_IX(M.g.guard, local / M.tiles_j, (M.g.nx + TI - 1) / TI),
+                  tj = local - (local / M.tiles_j) * M.tiles_j;
         StageArgs a;
         a.uin = st == 0 ? M.S : (st == 1 ? M.A : M.B);
         a.un = M.S;
@@ -331,7 +332,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         const long long npts = (long long)M.g.nx * M.g.ny;
         for (long long t = first + threadIdx.x; t < first + kPtChunk && t < npts; t += NT) {
           const int i = int(t / M.g.ny), j = int(t - (t / M.g.ny) * M.g.ny);
-          const long long p = (long long)(kGhost + i) * M.g.pitch + (kGhost + j);
+          const long long p = WENOFD_NODE(M.g, i, j);
 #pragma unroll
           for (int r = 0; r < 4; ++r) M.S[r * M.g.plane + p] = __ldcg(&M.A[r * M.g.plane + p]);
         }

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "cases.h"
+#include "guard.cuh"
 #include "solver.h"
 #include "trace.h"
 #include "wenofd_internal.h"
@@ -347,6 +348,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   cudaError_t e;
   if ((e = cudaSetDevice(device)) != cudaSuccess)
     return bail(fail(WENOFD_CUDA_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+  s->g.guard = wenofd::guard_record();  // the handle's device's (bounds-checked build)
   if ((e = cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(fail(WENOFD_CUDA_ERROR, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
   s->stream = s->own_stream;
@@ -410,6 +412,29 @@ namespace wenofd {
 // wenofd_last_error().
 void set_last_error(const std::string &msg) { g_error = msg; }
 }  // namespace wenofd
+
+namespace {
+
+// Guard record -> the public report, with the site's file name looked up
+// among the sources that hold guards.
+void guard_fill_report(const unsigned long long h[wenofd::kGuardWords], long long report[4], char *where,
+                       int where_len) {
+  static const char *const kFiles[] = {"aux_device.cuh", "aux_kernels.cu",   "batch_kernel.cuh", "learned.cu",
+                                       "learned_data.cu", "noalloc.cu",      "stage_f32.cuh",    "stage_kernel.cuh",
+                                       "guard.cuh",       "physics.cuh",     "tma.cuh"};
+  report[0] = (long long)h[wenofd::kGuardCount];
+  report[1] = h[wenofd::kGuardCount] ? (long long)(h[wenofd::kGuardSite] & 0xffffffffull) : 0;
+  report[2] = h[wenofd::kGuardCount] ? (long long)h[wenofd::kGuardIndex] : 0;
+  report[3] = h[wenofd::kGuardCount] ? (long long)h[wenofd::kGuardExtent] : 0;
+  if (!where || where_len <= 0 || !h[wenofd::kGuardCount]) return;
+  const unsigned hash = unsigned(h[wenofd::kGuardSite] >> 32);
+  const char *name = "?";
+  for (const char *f : kFiles)
+    if (wenofd::guard_file_hash(f) == hash) name = f;
+  std::snprintf(where, size_t(where_len), "%s:%lld", name, report[1]);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -999,6 +1024,40 @@ int wenofd_conservation_sums(wenofd_solver *s, double out[4]) {
   CUDA_TRY(cudaMemcpyAsync(s->red_host, s->red_out, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
   if (int rc = sync(s)) return rc;
   std::memcpy(out, s->red_host, 4 * sizeof(double));
+  return WENOFD_OK;
+}
+
+int wenofd_bounds_report(long long report[4], char *where, int where_len, int reset) {
+  if (!report) return fail(WENOFD_BAD_ARG, "null report");
+  if (where && where_len > 0) where[0] = '\0';
+  unsigned long long *rec = wenofd::guard_record();
+  if (!rec) {
+    report[0] = -1;
+    report[1] = report[2] = report[3] = 0;
+    return WENOFD_OK;
+  }
+  unsigned long long h[wenofd::kGuardWords] = {};
+  CUDA_TRY(cudaDeviceSynchronize());
+  CUDA_TRY(cudaMemcpy(h, rec, sizeof(h), cudaMemcpyDeviceToHost));
+  if (reset) CUDA_TRY(cudaMemset(rec, 0, sizeof(h)));
+  guard_fill_report(h, report, where, where_len);
+  return WENOFD_OK;
+}
+
+int wenofd_bounds_selftest(long long report[4], char *where, int where_len) {
+  if (!report) return fail(WENOFD_BAD_ARG, "null report");
+  if (where && where_len > 0) where[0] = '\0';
+  // a private record and the 4-element array, one allocation
+  unsigned long long *buf = nullptr;
+  CUDA_TRY(cudaMalloc(&buf, sizeof(unsigned long long) * wenofd::kGuardWords + 4 * sizeof(int)));
+  unsigned long long h[wenofd::kGuardWords] = {}, site = 0;
+  cudaError_t e = cudaMemset(buf, 0, sizeof(unsigned long long) * wenofd::kGuardWords + 4 * sizeof(int));
+  if (e == cudaSuccess)
+    e = wenofd::launch_guard_selftest(buf, reinterpret_cast<int *>(buf + wenofd::kGuardWords), &site, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(h, buf, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(buf);
+  if (e != cudaSuccess) return fail(WENOFD_CUDA_ERROR, std::string("bounds self-test: ") + cudaGetErrorString(e));
+  guard_fill_report(h, report, where, where_len);
   return WENOFD_OK;
 }
 

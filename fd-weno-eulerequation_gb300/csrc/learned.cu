@@ -18,6 +18,7 @@
 
 #include "../../include/wenofd.h"
 
+#include "guard.cuh"
 #include "learned_common.cuh"
 #include "trace.h"
 
@@ -54,10 +55,12 @@ __global__ void k_mlp_forward(const float *P, const float *X, long long n, float
 // given `part`, writes them to its own row there for an ordered sum.
 constexpr int kBB = 128;
 
-// rows: with idx set, sample s of the mini-batch is row idx[s] of X and Y.
+// rows: with idx set, sample s of the mini-batch is row idx[s] of X and Y
+// (rows of them in all).
 __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const float *X, const float *Y, long long n,
                                                       float inv_n, float *grad, float *loss, float *part,
-                                                      const long long *idx) {
+                                                      const long long *idx, long long rows,
+                                                      unsigned long long *guard) {
   extern __shared__ float sm[];
   float *sp = sm;                  // kParams
   float *sx = sp + kParams;        // kBB * kIn
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const floa
   for (int k = threadIdx.x; k < kBB * kIn; k += kBB) {
     const long long s = s0 + k / kIn;
     if (s >= n) sx[k] = 0.0f;
-    else if (idx) sx[k] = X[idx[s] * kIn + (k - (k / kIn) * kIn)];
+    else if (idx) sx[k] = X[WENOFD_IX(guard, idx[s], rows) * kIn + (k - (k / kIn) * kIn)];
     else sx[k] = X[s0 * kIn + k];
   }
   __syncthreads();
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(kBB) k_mlp_backward(const float *P, const floa
     sh2[t * kHid + o] = h;
     logit += sp[oW3 + o] * h;
   }
-  const float y = valid ? Y[idx ? idx[s0 + t] : s0 + t] : 0.0f;
+  const float y = valid ? Y[WENOFD_IX(guard, idx ? idx[s0 + t] : s0 + t, rows)] : 0.0f;
   const float pr = 1.0f / (1.0f + expf(-logit));
   const float d = valid ? (pr - y) * inv_n : 0.0f;
   sd[t] = d;
@@ -317,8 +320,12 @@ __device__ __forceinline__ unsigned gelu2_bf16x2(float z0, float z1) {
 
 // 2 x GELU of the 32 accumulator columns of this thread's row into columns
 // 0..31 of A2 [128 x 48], and columns 32..47 = 1, 1, 0, ... (bias inputs).
-__device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row) {
+// (rec: the guard record, bounds-checked build)
+__device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 *A, int row,
+                                               unsigned long long *rec) {
   constexpr int kc = kK2 / 8;
+  constexpr long long n = kCells * kK2;  // elements of A2
+  (void)n;
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     uint4 q;
@@ -326,10 +333,12 @@ __device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 
     q.y = gelu2_bf16x2(z[8 * c + 2], z[8 * c + 3]);
     q.z = gelu2_bf16x2(z[8 * c + 4], z[8 * c + 5]);
     q.w = gelu2_bf16x2(z[8 * c + 6], z[8 * c + 7]);
-    *reinterpret_cast<uint4 *>(&A[canon_off(row, 8 * c, kc)]) = q;
+    *reinterpret_cast<uint4 *>(&A[WENOFD_SPAN(rec, canon_off(row, 8 * c, kc), canon_off(row, 8 * c, kc) + 7, n)]) = q;
   }
-  *reinterpret_cast<uint4 *>(&A[canon_off(row, 32, kc)]) = make_uint4(0x3F803F80u, 0u, 0u, 0u);  // two BF16 1.0
-  *reinterpret_cast<uint4 *>(&A[canon_off(row, 40, kc)]) = make_uint4(0u, 0u, 0u, 0u);
+  *reinterpret_cast<uint4 *>(&A[WENOFD_SPAN(rec, canon_off(row, 32, kc), canon_off(row, 32, kc) + 7, n)]) =
+      make_uint4(0x3F803F80u, 0u, 0u, 0u);  // two BF16 1.0
+  *reinterpret_cast<uint4 *>(&A[WENOFD_SPAN(rec, canon_off(row, 40, kc), canon_off(row, 40, kc) + 7, n)]) =
+      make_uint4(0u, 0u, 0u, 0u);
 }
 
 // Normalised 5x5 window (normalise() in learned_common.cuh, same arithmetic)
@@ -337,7 +346,7 @@ __device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 
 // 16-byte chunks; columns col0+25 .. col0+31 take `tail` (two values, then
 // zeros).
 __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A, int row, int col0, float tail0,
-                                             float tail1) {
+                                             float tail1, unsigned long long *rec) {
   constexpr int kc = kK1 / 8;
   const float c = w[12];
   // differences and scaling on packed FP32 pairs (two operations per
@@ -374,7 +383,8 @@ __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A
     q.y = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 2), val(8 * ch + 3)));
     q.z = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 4), val(8 * ch + 5)));
     q.w = bf2_bits(__floats2bfloat162_rn(val(8 * ch + 6), val(8 * ch + 7)));
-    *reinterpret_cast<uint4 *>(&A[canon_off(row, col0 + 8 * ch, kc)]) = q;
+    const int o = canon_off(row, col0 + 8 * ch, kc);
+    *reinterpret_cast<uint4 *>(&A[WENOFD_SPAN(rec, o, o + 7, kCells * kK1)]) = q;
   }
 }
 
@@ -470,7 +480,7 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
         const int pi = row0 + k / kPJ, pj = k - (k / kPJ) * kPJ;
         const int ei = kGhost + i0 - 2 + pi, ej = kGhost + j0 - 2 + pj;
         ok[q] = k < count && ei < g.nxt && ej < g.nyt;
-        const double *src = U + (long long)ei * g.pitch + ej;
+        const double *src = U + WENOFD_GNODE_IF(g, ok[q], ei, ej);
 #pragma unroll
         for (int r = 0; r < 4; ++r) v[q][r] = ok[q] ? __ldg(src + r * g.plane) : 0.0;
       }
@@ -484,7 +494,7 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
             r = dev::f64_to_f32(v[q][0]);
             p = pressure32(gam, r, dev::f64_to_f32(v[q][1]), dev::f64_to_f32(v[q][2]), dev::f64_to_f32(v[q][3]));
           }
-          const int slot = ((i0 - 2 + pi) & (kPI - 1)) * kPJ + pj;
+          const int slot = WENOFD_IX(g.guard, ((i0 - 2 + pi) & (kPI - 1)) * kPJ + pj, kPI * kPJ);
           sRho[slot] = r;
           sPre[slot] = p;
         }
@@ -501,13 +511,13 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[rows[a] + b];
-      window_store(w, sA1, tid, 0, 1.0f, 1.0f);  // columns 25, 26: bias inputs
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[WENOFD_IX(g.guard, rows[a] + b, kPI * kPJ)];
+      window_store(w, sA1, tid, 0, 1.0f, 1.0f, g.guard);  // columns 25, 26: bias inputs
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
-        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[rows[a] + b];
-      window_store(w, sA1, tid, kColP, 0.0f, 0.0f);
+        for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[WENOFD_IX(g.guard, rows[a] + b, kPI * kPJ)];
+      window_store(w, sA1, tid, kColP, 0.0f, 0.0f, g.guard);
     }
     // 3. layer 1 (bias included)
     if (!layer([&] { mma_layer<kK1, kHid>(tmem, sA1, sB1); })) break;
@@ -515,7 +525,7 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
     {
       float z[32];
       tmem_ld32(tmem + lane_base, z);
-      gelu_row_store(z, sA2, tid);
+      gelu_row_store(z, sA2, tid, g.guard);
     }
     // 5. layer 2
     if (!layer([&] { mma_layer<kK2, kHid>(tmem + 32, sA2, sB2); })) break;
@@ -523,7 +533,7 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
     {
       float z[32];
       tmem_ld32(tmem + lane_base + 32, z);
-      gelu_row_store(z, sA2, tid);
+      gelu_row_store(z, sA2, tid, g.guard);
     }
     // 7. output layer on the tensor cores, into the columns of D1
     if (!layer([&] { mma_layer<kK2, kN3>(tmem, sA2, sB3); })) break;
@@ -533,7 +543,8 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
       const float logit = d[0] + d[1];
       const int i = i0 + warp, j = j0 + (tid & 31);
       if (i < g.nx && j < g.ny && !failed)
-        flags[(long long)(kGhost + i) * flag_pitch + (kGhost + j)] = logit > logit_threshold ? 1 : 0;
+        flags[WENOFD_IX(g.guard, (long long)(kGhost + i) * flag_pitch + (kGhost + j), (long long)g.nxt * flag_pitch)] =
+            logit > logit_threshold ? 1 : 0;
     }
     tc_fence_before();
     if (__syncthreads_or(failed)) break;
@@ -663,8 +674,9 @@ namespace {
 // gradients into grad / loss with atomics (after zeroing them); with part
 // (room for one row of kParams + 1 floats per block) they write partials and
 // k_grad_reduce sums them in block order.
+// (rows: the rows of x and y that idx indexes)
 int launch_backward(const float *params, const float *x, const float *y, long long n, float *grad, float *loss,
-                    float *part, cudaStream_t s, const long long *idx = nullptr) {
+                    float *part, cudaStream_t s, const long long *idx = nullptr, long long rows = 0) {
   using namespace wenofd::lrn;
   const size_t smem = sizeof(float) * (kParams + kBB * kIn + 4 * kBB * kHid + 2 * kBB);
   int dev = 0;
@@ -680,7 +692,8 @@ int launch_backward(const float *params, const float *x, const float *y, long lo
   if (!part && (cudaMemsetAsync(grad, 0, kParams * sizeof(float), s) != cudaSuccess ||
                 cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess))
     return WENOFD_CUDA_ERROR;
-  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(params, x, y, n, 1.0f / float(n), grad, loss, part, idx);
+  k_mlp_backward<<<int(blocks), kBB, smem, s>>>(params, x, y, n, 1.0f / float(n), grad, loss, part, idx,
+                                                idx ? rows : n, wenofd::guard_record());
   if (part) k_grad_reduce<<<(kParams + 1 + 255) / 256, 256, 0, s>>>(part, int(blocks), grad, loss);
   return cudaGetLastError() == cudaSuccess ? WENOFD_OK : WENOFD_CUDA_ERROR;
 }
@@ -752,7 +765,7 @@ extern "C" int wenofd_mlp_train(float *dev_params, const float *dev_x, const flo
     for (long long k = 0; k < nb && rc == WENOFD_OK; ++k) {
       const long long off = k * batch;
       const long long cnt = off + batch <= n ? batch : n - off;
-      rc = launch_backward(dev_params, dev_x, dev_y, cnt, grad, loss, part, s, perm_dev + off);
+      rc = launch_backward(dev_params, dev_x, dev_y, cnt, grad, loss, part, s, perm_dev + off, n);
       if (rc == WENOFD_OK) rc = wenofd_mlp_adam(dev_params, grad, m, v, ++step, lr, stream);
       if (rc == WENOFD_OK && host_epoch_loss && (k == nb - 1 || k % 16 == 0)) {
         float l = 0.0f;

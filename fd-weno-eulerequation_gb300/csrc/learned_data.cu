@@ -5,6 +5,7 @@
 //    (FP64, the training target).
 // Compiled with -fmad=false: features and labels then round exactly like the
 // oracle's restatement (oracle/wenofd_oracle.c), which tests hold them to.
+#include "guard.cuh"
 #include "learned_common.cuh"
 #include "physics.cuh"
 
@@ -17,11 +18,12 @@ namespace lrn {
 __device__ __forceinline__ void cell_features(const Geom &g, const double *U, long long c, float *row) {
   const float gam = float(g.gamma);
   {
+    c = WENOFD_IX(g.guard, c, (long long)g.nx * g.ny);
     const int i = int(c / g.ny), j = int(c - (c / g.ny) * g.ny);
     float wr[25], wp[25];
     for (int a = 0; a < 5; ++a)
       for (int b = 0; b < 5; ++b) {
-        const long long base = (long long)(kGhost + i + a - 2) * g.pitch + (kGhost + j + b - 2);
+        const long long base = WENOFD_GNODE(g, kGhost + i + a - 2, kGhost + j + b - 2);
         const float r = float(U[base]), mu = float(U[g.plane + base]), mv = float(U[2 * g.plane + base]),
                     E = float(U[3 * g.plane + base]);
         wr[a * 5 + b] = r;
@@ -154,8 +156,7 @@ __device__ double face_deviation(const Geom &g, const double *U, int ei, int ej)
   const int di = DIR == 0 ? 1 : 0, dj = DIR == 0 ? 0 : 1;
   double ave[4];
   for (int r = 0; r < 4; ++r)
-    ave[r] = 0.5 * (U[r * g.plane + (long long)(ei - di) * g.pitch + (ej - dj)] +
-                    U[r * g.plane + (long long)ei * g.pitch + ej]);
+    ave[r] = 0.5 * (U[r * g.plane + WENOFD_GNODE(g, ei - di, ej - dj)] + U[r * g.plane + WENOFD_GNODE(g, ei, ej)]);
   double u, v, p;
   dev::primitives<double>(g.gamma, ave, u, v, p);
   const double c = sqrt(g.gamma * p / ave[0]);
@@ -164,7 +165,7 @@ __device__ double face_deviation(const Geom &g, const double *U, int ei, int ej)
   double fp[6][4], fm[6][4];
   for (int s = 0; s < 6; ++s) {
     double q[4];
-    for (int r = 0; r < 4; ++r) q[r] = U[r * g.plane + (long long)(ei + (s - 3) * di) * g.pitch + (ej + (s - 3) * dj)];
+    for (int r = 0; r < 4; ++r) q[r] = U[r * g.plane + WENOFD_GNODE(g, ei + (s - 3) * di, ej + (s - 3) * dj)];
     dev::flux_split<double, DIR>(g.gamma, q, fm[s], fp[s]);
   }
   double vp[4][5], vm[4][5], scale = 0.0;

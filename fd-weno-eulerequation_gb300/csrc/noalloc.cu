@@ -35,6 +35,8 @@
 #include <mutex>
 #include <string>
 
+#include "guard.cuh"
+
 namespace {
 
 constexpr int kThreads = 256;
@@ -74,7 +76,7 @@ unsigned long long current_context_id() {
 // any node gave NaN.  This file is compiled without FMA contraction, so the
 // values round exactly as in the reference.
 __global__ void k_noalloc_block_max(const double *U, long long n, double dx, double dy, double gamma,
-                                    double *block_max) {
+                                    double *block_max, unsigned long long *guard) {
   double smax = 0.0;
   int nan_seen = 0;
   // a node whose four values are bit for bit those of the last node this
@@ -119,19 +121,19 @@ __global__ void k_noalloc_block_max(const double *U, long long n, double dx, dou
       m = wmax[w] > m ? wmax[w] : m;
       nn |= wnan[w];
     }
-    block_max[blockIdx.x] = nn ? __longlong_as_double(0x7ff8000000000000LL) : m;
+    block_max[WENOFD_IX(guard, blockIdx.x, kMaxBlocks)] = nn ? __longlong_as_double(0x7ff8000000000000LL) : m;
   }
 }
 
 // dt = min(1.0, cfl / max s), clipped to t_end - now (src/WENOFD.cpp:401,
 // 426-435); NaN when any node's wave speed was NaN (lines 437-442).
 __global__ void k_noalloc_finish(const double *block_max, int nblk, double cfl, double now, double t_end,
-                                 double *dt_out) {
+                                 double *dt_out, unsigned long long *guard) {
   if (threadIdx.x != 0) return;
   double m = 0.0;
   int nn = 0;
   for (int b = 0; b < nblk; ++b) {
-    const double x = block_max[b];
+    const double x = block_max[WENOFD_IX(guard, b, kMaxBlocks)];
     if (x != x) nn = 1;
     else if (x > m) m = x;
   }
@@ -193,8 +195,11 @@ extern "C" int wenofd_calc_dt_noalloc(const double *dev_state, int nx, int ny, d
   long long blocks = (n + kThreads - 1) / kThreads;
   if (blocks > kMaxBlocks) blocks = kMaxBlocks;
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
-  k_noalloc_block_max<<<int(blocks), kThreads, 0, s>>>(dev_state, n, dx, dy, gamma, scratch);
-  k_noalloc_finish<<<1, 32, 0, s>>>(scratch, int(blocks), cfl, now, t_end, dev_dt);
+  // (the bounds-checked build's guard record; null in the release build,
+  // which allocates nothing here)
+  unsigned long long *guard = wenofd::guard_record();
+  k_noalloc_block_max<<<int(blocks), kThreads, 0, s>>>(dev_state, n, dx, dy, gamma, scratch, guard);
+  k_noalloc_finish<<<1, 32, 0, s>>>(scratch, int(blocks), cfl, now, t_end, dev_dt, guard);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(WENOFD_CUDA_ERROR, std::string("launch: ") + cudaGetErrorString(e));
   return WENOFD_OK;

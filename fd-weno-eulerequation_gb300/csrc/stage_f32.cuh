@@ -255,8 +255,12 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       tma_bar_expect(bar, S::kBoxBytes + (ROUTE ? S::kFlagBoxBytes : 0u));
       // box column 0 = ghosted column j0 (even: 16-byte aligned); row 0 =
       // ghosted row 1 + i0, the first halo row
-      tma_load_3d(tma_smem_addr(base), &tma->u, j0, 1 + i0, 0, bar);
-      if constexpr (ROUTE) tma_load_2d(tma_smem_addr(sflag), &tma->flags, j0, 2 + i0, bar);
+      // first coordinates: x * element size a multiple of 16 bytes (an
+      // unissued copy leaves the wait below to give up)
+      if (WENOFD_REQUIRE(g.guard, (j0 & 1) == 0, j0, 2)) tma_load_3d(tma_smem_addr(base), &tma->u, j0, 1 + i0, 0, bar);
+      if constexpr (ROUTE)
+        if (WENOFD_REQUIRE(g.guard, (j0 & 15) == 0, j0, 16))
+          tma_load_2d(tma_smem_addr(sflag), &tma->flags, j0, 2 + i0, bar);
     }
   }
 
@@ -270,7 +274,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
         const int r = t / (TI * TJ), q = t - r * (TI * TJ);
         const int i = q / TJ, j = q - (q / TJ) * TJ;
         if (i0 + i < g.nx && j0 + j < g.ny)
-          cp_async8_f32(&Un64[t], &a.un[r * g.plane + (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j)]);
+          cp_async8_f32(&Un64[WENOFD_IX(g.guard, t, 4 * TI * TJ)], &a.un[r * g.plane + WENOFD_NODE(g, i0 + i, j0 + j)]);
       }
     }
   }
@@ -297,7 +301,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       const int hi = t / PJ, p = t - (t / PJ) * PJ;
       double2 v[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) v[r] = box[(r * HI + hi) * PJ + p];
+      for (int r = 0; r < 4; ++r) v[r] = box[WENOFD_IX(g.guard, (r * HI + hi) * PJ + p, S::kBoxBytes / 16)];
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int hj = 2 * p - 1 + h;
@@ -305,12 +309,13 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
         double x[4];
 #pragma unroll
         for (int r = 0; r < 4; ++r) x[r] = h ? v[r].y : v[r].x;
-        Us[hi * HJ + hj] = make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
+        Us[WENOFD_IX(g.guard, hi * HJ + hj, S::kU)] =
+            make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
         if constexpr (KEEP) {
           if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
             const int q = (hi - 3) * TJ + hj - 3;
 #pragma unroll
-            for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = x[r];
+            for (int r = 0; r < 4; ++r) U64[WENOFD_IX(g.guard, r * TI * TJ + q, 4 * TI * TJ)] = x[r];
           }
         }
       }
@@ -341,7 +346,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       const int hi = t / PJ, p = t - (t / PJ) * PJ;
       const int ei = 1 + i0 + hi, ej = j0 + 2 * p;
       const bool ok = t < HI * PJ && ei < g.nxt && ej < g.pitch;
-      const double2 *src = reinterpret_cast<const double2 *>(a.uin + (long long)ei * g.pitch + ej);
+      // (ej even and the pitch a multiple of 32: ej + 1 is in the row too)
+      const double2 *src = reinterpret_cast<const double2 *>(a.uin + WENOFD_GNODE_IF(g, ok, ei, ej));
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
         if constexpr (COH) v[k][r] = ok ? __ldcg(src + r * (g.plane / 2)) : make_double2(0.0, 0.0);
@@ -355,7 +361,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
         const int fi = t / WJ, w = t - (t / WJ) * WJ;
         const int ei = 2 + i0 + fi, ej = j0 + 4 * w;
         fv[k] = (t < FI * WJ && ei < g.nxt && ej < g.pitch)
-                    ? *reinterpret_cast<const unsigned *>(a.flags + (long long)ei * g.pitch + ej)
+                    ? *reinterpret_cast<const unsigned *>(a.flags + WENOFD_GNODE(g, ei, ej))
                     : 0x01010101u;
       }
     }
@@ -371,12 +377,13 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
           double x[4];
 #pragma unroll
           for (int r = 0; r < 4; ++r) x[r] = h ? v[k][r].y : v[k][r].x;
-          Us[hi * HJ + hj] = make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
+          Us[WENOFD_IX(g.guard, hi * HJ + hj, S::kU)] =
+              make_float4(f64_to_f32(x[0]), f64_to_f32(x[1]), f64_to_f32(x[2]), f64_to_f32(x[3]));
           if constexpr (KEEP) {
             if (hi >= 3 && hi < 3 + TI && hj >= 3 && hj < 3 + TJ) {
               const int q = (hi - 3) * TJ + hj - 3;
 #pragma unroll
-              for (int r = 0; r < 4; ++r) U64[r * TI * TJ + q] = x[r];
+              for (int r = 0; r < 4; ++r) U64[WENOFD_IX(g.guard, r * TI * TJ + q, 4 * TI * TJ)] = x[r];
             }
           }
         }
@@ -391,7 +398,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
             const int fj = 4 * w + c - 2;  // global column j0 + 4w + c = 2 + j0 + fj
-            if (fj >= 0 && fj < FJ) sflag[fi * FJ + fj] = (unsigned char)(fv[k] >> (8 * c));
+            if (fj >= 0 && fj < FJ) sflag[WENOFD_IX(g.guard, fi * FJ + fj, FI * FS)] = (unsigned char)(fv[k] >> (8 * c));
           }
         }
       }
@@ -404,7 +411,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   // --- x sweep: split fluxes of halo rows 0..HI-1, tile columns
   for (int t = threadIdx.x; t < HI * TJ; t += NT) {
     const int hi = t / TJ, j = t - (t / TJ) * TJ;
-    split4<0>(gamma, Us[hi * HJ + j + 3], Fm[t], Fp[t]);
+    split4<0>(gamma, Us[WENOFD_IX(g.guard, hi * HJ + j + 3, S::kU)], Fm[WENOFD_IX(g.guard, t, S::kSplit)],
+              Fp[WENOFD_IX(g.guard, t, S::kSplit)]);
   }
   __syncthreads();
   // x faces f = 0..TI between tile nodes f-1 and f: F+ rows f..f+4, F- rows f+1..f+5
@@ -412,12 +420,16 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     const int f = t / TJ, j = t - (t / TJ) * TJ;
     if (i0 + f > g.nx || j0 + j >= g.ny) continue;
     if constexpr (ROUTE) {
-      Hf[t] = linear_face4(Fp + t, Fm + t + TJ, TJ);
-      const unsigned char *fl = sflag + f * FS + (j + 2 + FO);  // nodes f-2 .. f+1
-      if (fl[0] | fl[FS] | fl[2 * FS] | fl[3 * FS]) slist[atomicAdd(&scount_x, 1)] = short(t);
+      Hf[WENOFD_IX(g.guard, t, S::kFace)] =
+          linear_face4(Fp + WENOFD_SPAN(g.guard, t, t + 4 * TJ, S::kSplit),
+                       Fm + WENOFD_SPAN(g.guard, t + TJ, t + 5 * TJ, S::kSplit), TJ);
+      // nodes f-2 .. f+1
+      const unsigned char *fl = sflag + WENOFD_SPAN(g.guard, f * FS + (j + 2 + FO), (f + 3) * FS + (j + 2 + FO), FI * FS);
+      if (fl[0] | fl[FS] | fl[2 * FS] | fl[3 * FS]) slist[WENOFD_IX(g.guard, atomicAdd(&scount_x, 1), kMaxFaces)] = short(t);
     } else {
-      Hf[t] = weno_face4<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3], Fp + t,
-                                    Fm + t + TJ, TJ);
+      Hf[WENOFD_IX(g.guard, t, S::kFace)] = weno_face4<0, SCHEME>(
+          gamma, zpl, Us[WENOFD_IX(g.guard, (f + 2) * HJ + j + 3, S::kU)], Us[WENOFD_IX(g.guard, (f + 3) * HJ + j + 3, S::kU)],
+          Fp + WENOFD_SPAN(g.guard, t, t + 4 * TJ, S::kSplit), Fm + WENOFD_SPAN(g.guard, t + TJ, t + 5 * TJ, S::kSplit), TJ);
     }
   }
   // The listed faces (if any) are recomputed with WENO after the barrier;
@@ -428,11 +440,13 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if (nw) {
       for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {  // 4 lanes per face, whole warps
         const int q4 = base + (threadIdx.x & 31);
-        const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
+        const int t = slist[WENOFD_IX(g.guard, q4 < 4 * nw ? q4 >> 2 : 0, kMaxFaces)];
         const int f = t / TJ, j = t - (t / TJ) * TJ;
-        const float o = weno_face_lane<0, SCHEME>(gamma, zpl, Us[(f + 2) * HJ + j + 3], Us[(f + 3) * HJ + j + 3],
-                                                  Fp + t, Fm + t + TJ, TJ, q4 & 3);
-        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+        const float o = weno_face_lane<0, SCHEME>(
+            gamma, zpl, Us[WENOFD_IX(g.guard, (f + 2) * HJ + j + 3, S::kU)], Us[WENOFD_IX(g.guard, (f + 3) * HJ + j + 3, S::kU)],
+            Fp + WENOFD_SPAN(g.guard, t, t + 4 * TJ, S::kSplit), Fm + WENOFD_SPAN(g.guard, t + TJ, t + 5 * TJ, S::kSplit), TJ,
+            q4 & 3);
+        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[WENOFD_IX(g.guard, t, S::kFace)])[q4 & 3] = o;
       }
       __syncthreads();
     }
@@ -446,7 +460,7 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   for (int k = 0; k < PPT; ++k) {
     const int t = threadIdx.x + k * NT;
     if (t < TI * TJ) {
-      const float4 hr = Hf[t + TJ], hl = Hf[t];
+      const float4 hr = Hf[WENOFD_IX(g.guard, t + TJ, S::kFace)], hl = Hf[WENOFD_IX(g.guard, t, S::kFace)];
       const float2 mi = splat2(-idx);  // -(hr - hl) * idx, the negation exact
       rhs[k] = join2(__fmul2_rn(sub2(lo2(hr), lo2(hl)), mi), __fmul2_rn(sub2(hi2(hr), hi2(hl)), mi));
     }
@@ -458,7 +472,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   // --- y sweep: split fluxes of tile rows, halo columns 0..HJ-1
   for (int t = threadIdx.x; t < TI * HJ; t += NT) {
     const int i = t / HJ, hj = t - (t / HJ) * HJ;
-    split4<1>(gamma, Us[(i + 3) * HJ + hj], Fm[t], Fp[t]);
+    split4<1>(gamma, Us[WENOFD_IX(g.guard, (i + 3) * HJ + hj, S::kU)], Fm[WENOFD_IX(g.guard, t, S::kSplit)],
+              Fp[WENOFD_IX(g.guard, t, S::kSplit)]);
   }
   __syncthreads();
   // y faces f = 0..TJ of row i: F+ columns f..f+4, F- columns f+1..f+5
@@ -467,12 +482,15 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if (i0 + i >= g.nx || j0 + f > g.ny) continue;
     const int s = i * HJ + f;
     if constexpr (ROUTE) {
-      Hf[t] = linear_face4(Fp + s, Fm + s + 1, 1);
-      const unsigned char *fl = sflag + (i + 2) * FS + f + FO;  // nodes f-2 .. f+1 along y
-      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[atomicAdd(&scount_y, 1)] = short(t);
+      Hf[WENOFD_IX(g.guard, t, S::kFace)] = linear_face4(Fp + WENOFD_SPAN(g.guard, s, s + 4, S::kSplit),
+                                                         Fm + WENOFD_SPAN(g.guard, s + 1, s + 5, S::kSplit), 1);
+      // nodes f-2 .. f+1 along y
+      const unsigned char *fl = sflag + WENOFD_SPAN(g.guard, (i + 2) * FS + f + FO, (i + 2) * FS + f + FO + 3, FI * FS);
+      if (fl[0] | fl[1] | fl[2] | fl[3]) slist[WENOFD_IX(g.guard, atomicAdd(&scount_y, 1), kMaxFaces)] = short(t);
     } else {
-      Hf[t] = weno_face4<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3], Fp + s,
-                                    Fm + s + 1, 1);
+      Hf[WENOFD_IX(g.guard, t, S::kFace)] = weno_face4<1, SCHEME>(
+          gamma, zpl, Us[WENOFD_IX(g.guard, (i + 3) * HJ + f + 2, S::kU)], Us[WENOFD_IX(g.guard, (i + 3) * HJ + f + 3, S::kU)],
+          Fp + WENOFD_SPAN(g.guard, s, s + 4, S::kSplit), Fm + WENOFD_SPAN(g.guard, s + 1, s + 5, S::kSplit), 1);
     }
   }
   __syncthreads();
@@ -481,12 +499,13 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if (nw) {
       for (int base = threadIdx.x & ~31; base < 4 * nw; base += NT) {
         const int q4 = base + (threadIdx.x & 31);
-        const int t = slist[q4 < 4 * nw ? q4 >> 2 : 0];
+        const int t = slist[WENOFD_IX(g.guard, q4 < 4 * nw ? q4 >> 2 : 0, kMaxFaces)];
         const int i = t / (TJ + 1), f = t - (t / (TJ + 1)) * (TJ + 1);
         const int s = i * HJ + f;
-        const float o = weno_face_lane<1, SCHEME>(gamma, zpl, Us[(i + 3) * HJ + f + 2], Us[(i + 3) * HJ + f + 3],
-                                                  Fp + s, Fm + s + 1, 1, q4 & 3);
-        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[t])[q4 & 3] = o;
+        const float o = weno_face_lane<1, SCHEME>(
+            gamma, zpl, Us[WENOFD_IX(g.guard, (i + 3) * HJ + f + 2, S::kU)], Us[WENOFD_IX(g.guard, (i + 3) * HJ + f + 3, S::kU)],
+            Fp + WENOFD_SPAN(g.guard, s, s + 4, S::kSplit), Fm + WENOFD_SPAN(g.guard, s + 1, s + 5, S::kSplit), 1, q4 & 3);
+        if (q4 < 4 * nw) reinterpret_cast<float *>(&Hf[WENOFD_IX(g.guard, t, S::kFace)])[q4 & 3] = o;
       }
       __syncthreads();
     }
@@ -511,25 +530,26 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
     if (t >= TI * TJ) continue;
     const int i = t / TJ, j = t - (t / TJ) * TJ;
     if (i0 + i >= g.nx || j0 + j >= g.ny) continue;
-    const float4 hr = Hf[i * (TJ + 1) + j + 1], hl = Hf[i * (TJ + 1) + j];
+    const float4 hr = Hf[WENOFD_IX(g.guard, i * (TJ + 1) + j + 1, S::kFace)],
+                 hl = Hf[WENOFD_IX(g.guard, i * (TJ + 1) + j, S::kFace)];
     const float2 mi = splat2(-idy);  // rhs - (hr - hl) * idy
     const float2 r01 = __ffma2_rn(sub2(lo2(hr), lo2(hl)), mi, lo2(rhs[k]));
     const float2 r23 = __ffma2_rn(sub2(hi2(hr), hi2(hl)), mi, hi2(rhs[k]));
     float rr[4] = {r01.x, r01.y, r23.x, r23.y};
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
-      const float4 q = Us[(i + 3) * HJ + j + 3];
+      const float4 q = Us[WENOFD_IX(g.guard, (i + 3) * HJ + j + 3, S::kU)];
       rr[3] += q.z * 1.0f;
       rr[2] += q.x * 1.0f;
     }
-    const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+    const long long gidx = WENOFD_NODE(g, i0 + i, j0 + j);
     double ui[4], un[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const long long ix = r * g.plane + gidx;
       if constexpr (KEEP) {
-        ui[r] = U64[r * TI * TJ + t];
+        ui[r] = U64[WENOFD_IX(g.guard, r * TI * TJ + t, 4 * TI * TJ)];
         if constexpr (COH) un[r] = __ldcg(&a.un[ix]);
-        else un[r] = Un64[r * TI * TJ + t];
+        else un[r] = Un64[WENOFD_IX(g.guard, r * TI * TJ + t, 4 * TI * TJ)];
       } else if constexpr (COH) {
         ui[r] = __ldcg(&a.uin[ix]);
         un[r] = __ldcg(&a.un[ix]);
@@ -570,7 +590,8 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
       float2 b = sred[0];
 #pragma unroll
       for (int w = 1; w < NT / 32; ++w) b = make_float2(fmaxf(b.x, sred[w].x), fmaxf(b.y, sred[w].y));
-      a.bounds[tile] = b;
+      // (allocated for tiles of 15 rows, the most tiles)
+      a.bounds[WENOFD_IX(g.guard, tile, ((g.nx + 14) / 15) * ((g.ny + 31) / 32))] = b;
       atomicMax(a.screen, __float_as_uint(b.x));
     }
   }

@@ -72,14 +72,13 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
       const int hi = rem / HJ, hj = rem - hi * HJ;
       const int ei = 1 + i0 + hi, ej = 1 + j0 + hj;
       const bool ok = t < 4 * HI * HJ && ei < g.nxt && ej < g.nyt;
-      const double *src = &a.uin[r * g.plane + (long long)ei * g.pitch + ej];
-      if constexpr (COH) v[k] = ok ? __ldcg(src) : 0.0;
-      else v[k] = ok ? __ldg(src) : 0.0;
+      if constexpr (COH) v[k] = ok ? __ldcg(&a.uin[WENOFD_STATE(g, r * g.plane + WENOFD_GNODE(g, ei, ej))]) : 0.0;
+      else v[k] = ok ? __ldg(&a.uin[WENOFD_STATE(g, r * g.plane + WENOFD_GNODE(g, ei, ej))]) : 0.0;
     }
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
-      if (t < 4 * HI * HJ) Us[t] = v[k];
+      if (t < 4 * HI * HJ) Us[WENOFD_IX(g.guard, t, S::kU)] = v[k];
     }
   }
   __syncthreads();
@@ -89,12 +88,12 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     const int hi = t / TJ, j = t - hi * TJ;
     T q[4], fm[4], fp[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) q[r] = Us[(r * HI + hi) * HJ + j + 3];
+    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, (r * HI + hi) * HJ + j + 3, S::kU)];
     flux_split<T, 0>(gamma, q, fm, fp);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      Fp[(r * HI + hi) * TJ + j] = fp[r];
-      Fm[(r * HI + hi) * TJ + j] = fm[r];
+      Fp[WENOFD_IX(g.guard, (r * HI + hi) * TJ + j, S::kSplit)] = fp[r];
+      Fm[WENOFD_IX(g.guard, (r * HI + hi) * TJ + j, S::kSplit)] = fm[r];
     }
   }
   __syncthreads();
@@ -105,12 +104,16 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     T um[4], u0[4], out[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      um[r] = Us[(r * HI + f + 2) * HJ + j + 3];
-      u0[r] = Us[(r * HI + f + 3) * HJ + j + 3];
+      um[r] = Us[WENOFD_IX(g.guard, (r * HI + f + 2) * HJ + j + 3, S::kU)];
+      u0[r] = Us[WENOFD_IX(g.guard, (r * HI + f + 3) * HJ + j + 3, S::kU)];
     }
-    face_flux<T, 0, SCHEME>(gamma, zpl, um, u0, Fp + f * TJ + j, Fm + (f + 1) * TJ + j, TJ, HI * TJ, out);
+    // stencils: nodes 0..4 TJ apart, components HI TJ apart
+    face_flux<T, 0, SCHEME>(gamma, zpl, um, u0,
+                            Fp + WENOFD_SPAN(g.guard, f * TJ + j, f * TJ + j + 4 * TJ + 3 * HI * TJ, S::kSplit),
+                            Fm + WENOFD_SPAN(g.guard, (f + 1) * TJ + j, (f + 5) * TJ + j + 3 * HI * TJ, S::kSplit),
+                            TJ, HI * TJ, out);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) Hf[(r * (TI + 1) + f) * TJ + j] = out[r];
+    for (int r = 0; r < 4; ++r) Hf[WENOFD_IX(g.guard, (r * (TI + 1) + f) * TJ + j, S::kFace)] = out[r];
   }
   __syncthreads();
 
@@ -125,7 +128,8 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       if (t < TI * TJ) {
-        const T hr = Hf[(r * (TI + 1) + i + 1) * TJ + j], hl = Hf[(r * (TI + 1) + i) * TJ + j];
+        const T hr = Hf[WENOFD_IX(g.guard, (r * (TI + 1) + i + 1) * TJ + j, S::kFace)],
+                hl = Hf[WENOFD_IX(g.guard, (r * (TI + 1) + i) * TJ + j, S::kFace)];
         rhs[k][r] = T(0.0) + tdiv(-(hr - hl), dx);
       }
     }
@@ -137,12 +141,12 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     const int i = t / HJ, hj = t - i * HJ;
     T q[4], fm[4], fp[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) q[r] = Us[(r * HI + i + 3) * HJ + hj];
+    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + hj, S::kU)];
     flux_split<T, 1>(gamma, q, fm, fp);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      Fp[(r * TI + i) * HJ + hj] = fp[r];
-      Fm[(r * TI + i) * HJ + hj] = fm[r];
+      Fp[WENOFD_IX(g.guard, (r * TI + i) * HJ + hj, S::kSplit)] = fp[r];
+      Fm[WENOFD_IX(g.guard, (r * TI + i) * HJ + hj, S::kSplit)] = fm[r];
     }
   }
   __syncthreads();
@@ -152,12 +156,16 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     T um[4], u0[4], out[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      um[r] = Us[(r * HI + i + 3) * HJ + f + 2];
-      u0[r] = Us[(r * HI + i + 3) * HJ + f + 3];
+      um[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + f + 2, S::kU)];
+      u0[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + f + 3, S::kU)];
     }
-    face_flux<T, 1, SCHEME>(gamma, zpl, um, u0, Fp + i * HJ + f, Fm + i * HJ + f + 1, 1, TI * HJ, out);
+    // stencils: nodes 0..4 adjacent, components TI HJ apart
+    face_flux<T, 1, SCHEME>(gamma, zpl, um, u0,
+                            Fp + WENOFD_SPAN(g.guard, i * HJ + f, i * HJ + f + 4 + 3 * TI * HJ, S::kSplit),
+                            Fm + WENOFD_SPAN(g.guard, i * HJ + f + 1, i * HJ + f + 5 + 3 * TI * HJ, S::kSplit), 1,
+                            TI * HJ, out);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) Hf[(r * TI + i) * (TJ + 1) + f] = out[r];
+    for (int r = 0; r < 4; ++r) Hf[WENOFD_IX(g.guard, (r * TI + i) * (TJ + 1) + f, S::kFace)] = out[r];
   }
   __syncthreads();
 
@@ -172,14 +180,15 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     T rr[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const T hr = Hf[(r * TI + i) * (TJ + 1) + j + 1], hl = Hf[(r * TI + i) * (TJ + 1) + j];
+      const T hr = Hf[WENOFD_IX(g.guard, (r * TI + i) * (TJ + 1) + j + 1, S::kFace)],
+              hl = Hf[WENOFD_IX(g.guard, (r * TI + i) * (TJ + 1) + j, S::kFace)];
       rr[r] = rhs[k][r] + tdiv(-(hr - hl), dy);
     }
-    const long long gidx = (long long)(4 + i0 + i) * g.pitch + (4 + j0 + j);
+    const long long gidx = WENOFD_NODE(g, i0 + i, j0 + j);
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
       const T g_g0 = T(1.0);
-      rr[3] += Us[(2 * HI + i + 3) * HJ + j + 3] * g_g0;
-      rr[2] += Us[(0 * HI + i + 3) * HJ + j + 3] * g_g0;
+      rr[3] += Us[WENOFD_IX(g.guard, (2 * HI + i + 3) * HJ + j + 3, S::kU)] * g_g0;
+      rr[2] += Us[WENOFD_IX(g.guard, (0 * HI + i + 3) * HJ + j + 3, S::kU)] * g_g0;
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {

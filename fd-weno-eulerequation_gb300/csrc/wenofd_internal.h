@@ -31,6 +31,9 @@ struct Geom {
   int gravity;                  // RTI source term (src/WENOFD.cpp:800-821)
   // FP32-form constants, rounded once on the host: gamma, zp_lambda, 1/dx, 1/dy
   float gamma32, zpl32, inv_dx32, inv_dy32;
+  // Bounds-checked build: the device guard record of this device
+  // (guard.cuh); null in the release build.
+  unsigned long long *guard;
 };
 
 // Device-resident control block of the time loop.  All fields are written
@@ -109,6 +112,14 @@ __host__ __device__ inline int rk_form(double a, double b, double c, const doubl
 
 Geom make_geom(int nx, int ny, double dx, double dy, double gamma, double zp_lambda, int bc_left,
                int bc_right, int bc_y, int gravity);
+// Bounds-checked build: the current device's guard record (guard.cuh),
+// kGuardWords words allocated and zeroed on first use; null in the release
+// build.
+unsigned long long *guard_record();
+// The guard self-test kernel (aux_kernels.cu): one guarded access one past
+// the end of buf[4], recorded in rec (kGuardWords words); returns the
+// self-test's source site.
+cudaError_t launch_guard_selftest(unsigned long long *rec, int *buf, unsigned long long *site, cudaStream_t s);
 
 // stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form,
 // routed by a.flags when it is set)
@@ -157,6 +168,8 @@ struct BatchArgs {
   // Test instance only (k_batch with WITHHOLD): block `hold_block` skips its
   // arrival at the launch's barrier number `hold_barrier` (counted from 0).
   int hold_block = -1, hold_barrier = -1;
+  // Bounds-checked build: the guard record (null in the release build).
+  unsigned long long *guard = nullptr;
 };
 
 // Per-member summary gathered for the host in one copy.

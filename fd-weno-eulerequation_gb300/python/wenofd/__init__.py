@@ -18,7 +18,9 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-LIB_PATH = os.path.join(PKG, "_build", "libwenofd.so")
+# WENOFD_LIBRARY selects another build of the library, e.g. the bounds-checked
+# one (_build_check/libwenofd.so, build.py --bounds-check).
+LIB_PATH = os.environ.get("WENOFD_LIBRARY") or os.path.join(PKG, "_build", "libwenofd.so")
 
 OK, BAD_CONFIG, CUDA_ERROR, NAN_DT, TIMEOUT, BAD_ARG, NO_EXACT = range(7)
 FP64, FP32, LEARNED = 0, 1, 2
@@ -114,6 +116,8 @@ def lib() -> C.CDLL:
         L.wenofd_mlp_init.argtypes = [C.POINTER(C.c_float), C.c_ulonglong]
         L.wenofd_save_state.argtypes = [H, C.c_char_p]
         L.wenofd_load_state.argtypes = [H, C.c_char_p]
+        L.wenofd_bounds_report.argtypes = [C.POINTER(C.c_longlong), C.c_char_p, C.c_int, C.c_int]
+        L.wenofd_bounds_selftest.argtypes = [C.POINTER(C.c_longlong), C.c_char_p, C.c_int]
         for f in ("wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
                   "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold"):
             getattr(L, f).restype = C.c_int
@@ -125,7 +129,7 @@ def lib() -> C.CDLL:
                   "wenofd_time_stages", "wenofd_calc_dt_noalloc", "wenofd_set_boundary_values",
                   "wenofd_set_indicator", "wenofd_indicator_flags", "wenofd_routing_flags", "wenofd_indicator_data",
                   "wenofd_mlp_forward", "wenofd_output_variables", "wenofd_save_state", "wenofd_load_state",
-                  "wenofd_indicator_sample", "wenofd_mlp_init",
+                  "wenofd_indicator_sample", "wenofd_mlp_init", "wenofd_bounds_report", "wenofd_bounds_selftest",
                   "wenofd_mlp_backward", "wenofd_mlp_adam", "wenofd_mlp_train"):
             getattr(L, f).restype = C.c_int
         _lib = L
@@ -370,6 +374,7 @@ EXPORTED = [
     "wenofd_batch_create", "wenofd_batch_destroy", "wenofd_batch_configure", "wenofd_batch_autotune",
     "wenofd_batch_advance", "wenofd_batch_get_info", "wenofd_batch_test_withhold", "wenofd_output_variables",
     "wenofd_save_state", "wenofd_load_state", "wenofd_indicator_sample", "wenofd_mlp_init",
+    "wenofd_bounds_report", "wenofd_bounds_selftest",
 ]
 
 
@@ -402,3 +407,22 @@ def mlp_train(params_ptr: int, x_ptr: int, y_ptr: int, n: int, epochs: int, batc
     _check(lib().wenofd_mlp_train(C.c_void_p(params_ptr), C.c_void_p(x_ptr), C.c_void_p(y_ptr), n, epochs, batch,
                                   lr, seed, losses.ctypes.data_as(C.POINTER(C.c_float)), C.c_void_p(stream)))
     return losses
+
+
+def bounds_report(reset: bool = False) -> dict:
+    """The device guard record of the bounds-checked library
+    (wenofd_bounds_report): count (-1 in the release library), and the first
+    violation's line, index, extent and "file:line"."""
+    r = (C.c_longlong * 4)()
+    where = C.create_string_buffer(128)
+    _check(lib().wenofd_bounds_report(r, where, 128, 1 if reset else 0))
+    return {"count": r[0], "line": r[1], "index": r[2], "extent": r[3], "where": where.value.decode()}
+
+
+def bounds_selftest() -> dict:
+    """One guarded access one past the end of a 4-element array against a
+    private record (wenofd_bounds_selftest), reported like bounds_report."""
+    r = (C.c_longlong * 4)()
+    where = C.create_string_buffer(128)
+    _check(lib().wenofd_bounds_selftest(r, where, 128))
+    return {"count": r[0], "line": r[1], "index": r[2], "extent": r[3], "where": where.value.decode()}

@@ -319,6 +319,28 @@ int wenofd_batch_test_withhold(wenofd_batch *b, int block, int barrier);
 int wenofd_calc_dt_noalloc(const double *dev_state, int nx, int ny, double dx, double dy, double gamma,
                            double cfl, double now, double t_end, double *dev_dt, void *stream);
 
+/* Index guards of the bounds-checked debug library (built with
+ * `python fd-weno-eulerequation_gb300/build.py --bounds-check`, i.e. with
+ * -DWENOFD_BOUNDS_CHECK, into fd-weno-eulerequation_gb300/_build_check/).  It
+ * stands in for the reference's assert-checked Array1D/Array2D indexing
+ * (utils/array.h:273-303, 552-583): every kernel tests its state, flag, table,
+ * work-item and shared-memory indices, and the TMA boxes' first coordinates,
+ * against their extents; an index out of range is counted in the current
+ * device's guard record and not used (the access goes to element 0 of the
+ * same array).  report[0] = violations since the last reset, report[1] = the
+ * first one's source line, report[2] = its index, report[3] = the extent (or
+ * alignment) it broke; `where` (if not null, where_len bytes) receives the
+ * first one's "file:line".  Waits for the device to finish its work first;
+ * reset != 0 zeroes the record afterwards.  In the release library
+ * report[0] = -1 (no guards compiled) and report[1..3] = 0. */
+int wenofd_bounds_report(long long report[4], char *where, int where_len, int reset);
+
+/* The guard mechanism itself, in either library: one kernel makes one guarded
+ * access one past the end of a 4-element array (the guard sends it to
+ * element 0) against a private record, returned as in wenofd_bounds_report:
+ * report = {1, line, 4, 4}, `where` naming the self-test's source line. */
+int wenofd_bounds_selftest(long long report[4], char *where, int where_len);
+
 #ifdef __cplusplus
 }
 #endif

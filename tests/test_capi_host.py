@@ -83,3 +83,18 @@ def test_mlp_init_is_seeded_and_scaled():
     assert np.abs(w2).max() <= np.sqrt(6 / 32) and np.abs(w3).max() <= np.sqrt(6 / 32)
     assert not b1.any() and not b2.any() and b3 == 0.0
     assert abs(float(w1.mean())) < 0.05
+
+
+def test_bounds_report_release_and_checked_exports():
+    """The release library reports no guards (count -1, no GPU needed); the
+    bounds-checked debug library, when built, exports the same ABI."""
+    import ctypes
+
+    rep = wenofd.bounds_report()
+    assert rep["count"] == -1 and rep["where"] == ""
+    checked = os.path.join(ROOT, "fd-weno-eulerequation_gb300", "_build_check", "libwenofd.so")
+    if not os.path.exists(checked):
+        pytest.skip("bounds-checked library not built (build.py --bounds-check)")
+    L = ctypes.CDLL(checked)
+    for name in wenofd.EXPORTED:
+        assert hasattr(L, name), name
