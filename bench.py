@@ -244,8 +244,9 @@ def time_form(wenofd, torch, precision: int, device: int, steps: int, warmup: in
 
 def kernel_tour(wenofd, torch, device: int, n: int) -> dict:
     """Every kernel of the path once, untimed, at n^2 (shear layer): the plain
-    FP64 and FP32 forms one RK3 step each with their time-step reductions and
-    conservation sums; one FP64 WENO-JS step of the smooth wave and its
+    FP64 and FP32 forms one RK3 step each with their time-step reductions,
+    conservation sums and output variables; one FP64 RK1 step and the time step
+    without allocation on its state; one FP64 WENO-JS step of the smooth wave and its
     density error norms; the learned form's data
     extraction, one training epoch on that data, and one step with the
     trained indicator; one step of a two-member FP32 and FP64 batch."""
@@ -255,7 +256,18 @@ def kernel_tour(wenofd, torch, device: int, n: int) -> dict:
     for name, prec in (("fp64", wenofd.FP64), ("fp32", wenofd.FP32)):
         with wenofd.Solver(dict(config_for(prec, device), ELEMNUMX=n, ELEMNUMY=n)) as s:
             s.initialize()
-            ran[name] = {"steps": s.advance(max_steps=1), "mass": float(s.conservation_sums()[0])}
+            ran[name] = {"steps": s.advance(max_steps=1), "mass": float(s.conservation_sums()[0]),
+                         "rho_max": float(s.output_variables()[0].max())}
+    with wenofd.Solver(dict(config_for(wenofd.FP64, device), ELEMNUMX=n, ELEMNUMY=n, RKMETH=0)) as s:
+        s.initialize()  # RK1: the stage buffer's interior copied back (k_copy_interior)
+        ran["fp64_rk1"] = {"steps": s.advance(max_steps=1)}
+        U = torch.from_numpy(s.get_state()).cuda(device)
+        dt = torch.zeros(1, dtype=torch.float64, device=f"cuda:{device}")
+        info = s.info()
+        rc = wenofd.lib().wenofd_calc_dt_noalloc(U.data_ptr(), n, n, info.dx, info.dy, info.gamma, 0.7, 0.0, 1.0,
+                                                 dt.data_ptr(), None)
+        torch.cuda.synchronize(device)
+        ran["noalloc_dt"] = {"rc": rc, "dt": float(dt.item())}
     with wenofd.Solver({"TESTCASE": 0, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.05, "SCHEME": 0,
                         "DEVICE": device}) as s:  # smooth wave: the error norms against its exact solution
         s.initialize()

@@ -61,6 +61,7 @@ def test_kernel_tour_runs():
     assert r.returncode == 0, r.stderr[-2000:]
     d = json.loads(r.stdout.strip().splitlines()[-1])
     tour = d["kernel_tour"]
-    for k in ("fp64", "fp32", "wave_fp64", "learned", "batch_fp32", "batch_fp64"):
+    for k in ("fp64", "fp32", "fp64_rk1", "wave_fp64", "learned", "batch_fp32", "batch_fp64"):
         assert tour[k]["steps"] == 1, k
     assert 0.0 <= tour["learned"]["flagged"] <= 1.0
+    assert tour["noalloc_dt"]["rc"] == 0 and tour["noalloc_dt"]["dt"] > 0.0
