@@ -210,6 +210,9 @@ __device__ __forceinline__ void cp_async8_f32(void *smem, const void *gmem) {
                : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all_f32() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// Asks L2 for the 128-byte line holding p (a hint: no data moves to the
+// thread, and nothing waits for it).
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.L2 [%0];" ::"l"(p)); }
 
 // One tile (TI x TJ interior nodes from i0, j0) of one RK stage, all NT
 // threads of the block.  ROUTE: faces take the linear upwind flux unless a
@@ -266,6 +269,25 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
 
   const float gamma = g.gamma32, zpl = g.zpl32;
   const bool stage1 = a.form == kFormStage1;
+
+  // Stages 2 and 3 without KEEP read U^n only in the epilogue, the first
+  // touch of those lines in this launch: ask L2 for them now, so that the
+  // epilogue's loads hit L2 instead of waiting on DRAM.  A tile row of 32
+  // doubles from ghosted column j0 + 4 (rows start on 256-byte boundaries,
+  // j0 a multiple of 32) spans three 128-byte lines, holding the tile's
+  // columns -4..11, 12..27 and 28..43: one prefetch at columns 0, 12 and 28
+  // (clamped to the grid) per row and component.
+  if constexpr (!COH && !KEEP) {
+    if (a.mode == kModeRK && !stage1) {
+      constexpr int kLines = 3;
+      for (int t = threadIdx.x; t < 4 * TI * kLines; t += NT) {
+        const int r = t / (TI * kLines), q = t - r * (TI * kLines);
+        const int i = q / kLines, l = q - (q / kLines) * kLines;
+        const int ii = min(i0 + i, g.nx - 1), jj = min(j0 + (l == 0 ? 0 : (l == 1 ? 12 : 28)), g.ny - 1);
+        prefetch_l2(&a.un[r * g.plane + WENOFD_NODE(g, ii, jj)]);
+      }
+    }
+  }
 
   // stages 2 and 3: fetch this tile's U^n now, used only by the epilogue
   if constexpr (!COH && KEEP) {
