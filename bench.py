@@ -403,23 +403,36 @@ BATCH_SHAPES = [(128, 128), (256, 256), (512, 512), (1024, 1024), (192, 320), (3
 BATCH_MEMBERS = 64
 
 
-def batching_leg(wenofd, precision: int, device: int, steps: int, warmup: int) -> dict:
+def batching_leg(wenofd, precision: int, device: int, steps: int, warmup: int, params=None, threshold: float = 0.5,
+                 interval: int = 1) -> dict:
     """Aggregate cell-updates/s of BATCH_MEMBERS independent solves of uneven
     sizes: one persistent kernel per launch (wenofd_batch_advance, autotuned)
     against the same solves advanced one at a time (wenofd_advance each,
     CUDA-graph replays).  Wall clock around the whole advance calls (host
     checks included in both arms); afterwards the batched members' states are
-    compared with the one-at-a-time states."""
+    compared with the one-at-a-time states.  The learned form (params: the
+    trained indicator) runs the batched indicator every `interval` steps
+    between batched launches, the single solves their own indicator; its
+    members are seeded shear layers (the workload the learned form is
+    specified on) of the same shapes: on seeded four-quadrant Riemann
+    problems the trained indicator at the bench's threshold misses shock faces
+    of some members, whose solves then stop with a NaN time step."""
     import numpy as np
 
     shapes = [BATCH_SHAPES[k % len(BATCH_SHAPES)] for k in range(BATCH_MEMBERS)]
+    testcase = 5 if precision == wenofd.LEARNED else 4
 
     def make():
         out = []
         for k, (nx, ny) in enumerate(shapes):
-            s = wenofd.Solver({"TESTCASE": 4, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
-                               "SEED": 1000 + k, "PRECISION": precision, "DEVICE": device})
+            cfg = {"TESTCASE": testcase, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
+                   "SEED": 1000 + k, "PRECISION": precision, "DEVICE": device}
+            if precision == wenofd.LEARNED:
+                cfg["INDICATOR_INTERVAL"] = interval
+            s = wenofd.Solver(cfg)
             s.initialize()
+            if precision == wenofd.LEARNED:
+                s.set_indicator(params, threshold)
             out.append(s)
         return out
 
@@ -441,15 +454,25 @@ def batching_leg(wenofd, precision: int, device: int, steps: int, warmup: int) -
     t_batch = time.perf_counter() - t0
     info = b.info()
     diff, l1 = 0.0, 0.0
+    flagged, flags_differ = 0.0, 0
     for m, a in zip(members, alone):
         Um, Ua = m.get_state(), a.get_state()
         diff = max(diff, float(np.max(np.abs(Um - Ua)) / np.max(np.abs(Ua))))
         l1 = max(l1, float(np.mean(np.abs(Um - Ua)) / np.mean(np.abs(Ua))))
+        if precision == wenofd.LEARNED:
+            fm, fa = m.routing_flags(), a.routing_flags()
+            flagged += float(fm.sum())
+            flags_differ += int(np.count_nonzero(fm != fa))
     b.close()
     for s in alone + members:
         s.close()
-    return {"members": BATCH_MEMBERS, "cells": cells, "steps": steps,
-            "shapes": "seeded Riemann, " + ", ".join(f"{nx}x{ny}" for nx, ny in BATCH_SHAPES) + " (x8 each)",
+    learned_keys = {}
+    if precision == wenofd.LEARNED:
+        learned_keys = {"indicator_interval": interval, "threshold": threshold, "flagged_fraction": flagged / cells,
+                        "routing_flags_differing_from_one_at_a_time": flags_differ}
+    return {**learned_keys, "members": BATCH_MEMBERS, "cells": cells, "steps": steps,
+            "shapes": ("seeded shear layers, " if testcase == 5 else "seeded Riemann, ") +
+            ", ".join(f"{nx}x{ny}" for nx, ny in BATCH_SHAPES) + " (x8 each)",
             "batched": {"value": steps * cells / t_batch, "unit": "cell-updates/s", "ms_per_step": 1e3 * t_batch / steps},
             "one_at_a_time": {"value": steps * cells / t_alone, "unit": "cell-updates/s",
                               "ms_per_step": 1e3 * t_alone / steps},
@@ -482,7 +505,7 @@ def main() -> None:
     ap.add_argument("--indicator-interval", type=int, default=INDICATOR_INTERVAL,
                     help="time steps per indicator run in the time loop")
     ap.add_argument("--only-batching", action="store_true",
-                    help="run the batching leg only (FP32 and FP64 batches vs one at a time): for profiling")
+                    help="run the batching leg only (FP32, learned and FP64 batches vs one at a time): for profiling")
     ap.add_argument("--only-fp32", action="store_true",
                     help="time the FP32 form only (no training, no other legs): for profiling")
     ap.add_argument("--only-headline", action="store_true",
@@ -543,7 +566,10 @@ def main() -> None:
                               "note": "FP32 form only (profiling run)"}))
         return
     if args.only_batching:
+        params, _ = train_indicator(torch, local)
         out = {"fp32": batching_leg(wenofd, wenofd.FP32, local, args.steps, args.warmup),
+               "learned_fp32": batching_leg(wenofd, wenofd.LEARNED, local, args.steps, args.warmup, params,
+                                            args.threshold, args.indicator_interval),
                "fp64": batching_leg(wenofd, wenofd.FP64, local, 2, args.warmup)}
         if rank == 0:
             print(json.dumps({"batching": out, "note": "batching leg only (profiling run)"}))
@@ -644,6 +670,8 @@ def main() -> None:
     batching = None
     if not args.no_batching:
         batching = {"fp32": batching_leg(wenofd, wenofd.FP32, local, args.steps, args.warmup),
+                    "learned_fp32": batching_leg(wenofd, wenofd.LEARNED, local, args.steps, args.warmup, params,
+                                                 args.threshold, args.indicator_interval),
                     "fp64": batching_leg(wenofd, wenofd.FP64, local, 2, args.warmup)}
 
     cb = None

@@ -46,6 +46,7 @@ CUDA_UNITS = {
     "learned.cu": ["-prec-sqrt=false", "-prec-div=false"],
     "batch_fp64.cu": ["-fmad=false"],
     "batch_fp32.cu": ["-prec-sqrt=false"],
+    "batch_learned.cu": ["-prec-sqrt=false"],
 }
 CXX_UNITS = ["capi.cpp", "cases.cpp", "batch.cpp"]
 

@@ -10,6 +10,18 @@
 namespace wenofd {
 namespace dev {
 
+// Member owning work item `item` of a batch's prefix array (n+1 entries).
+// The prefix arrays and the member table are read-only for the whole launch.
+__device__ __forceinline__ int owner(const int *prefix, int n, int item) {
+  int lo = 0, hi = n;  // prefix[lo] <= item < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&prefix[mid]) <= item) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 __device__ __forceinline__ long long at(const Geom &g, int r, int ei, int ej) {
   return WENOFD_IXC(g.guard, unsigned(r) < 4u && unsigned(ei) < unsigned(g.nxt) && unsigned(ej) < unsigned(g.pitch),
                     r * g.plane + (long long)ei * g.pitch + ej, 4 * g.plane);

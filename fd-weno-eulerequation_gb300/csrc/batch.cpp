@@ -6,11 +6,20 @@
 // A batch holds no state of its own beyond its work plan: the members'
 // device arrays and control blocks are the ones their handles own, so a
 // member's results and time are read through its own handle.
+//
+// Learned-form batches alternate two launches: the batched tensor-core
+// indicator over every member's U^n (learned.cu), then the batched kernel
+// for INDICATOR_INTERVAL steps routed by those flags, whose launch ends with
+// the ghost fill the next indicator run reads.  An advance call starts with
+// a launch of no steps that fills the ghosts, so the indicator runs on the
+// first step of every call and then every INDICATOR_INTERVAL steps, as in
+// the single solve.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/wenofd.h"
@@ -25,21 +34,30 @@ using wenofd::Ctrl;
 
 struct wenofd_batch {
   int device = 0, n = 0, precision = 0, scheme = 0, rk = 2;
+  // learned form: indicator runs every `interval` steps
+  bool learned = false;
+  int interval = 1;
   std::vector<wenofd_solver *> members;
   cudaStream_t stream = nullptr;
   // work plan (device)
   BatchMember *d_members = nullptr;
-  int *d_prefix = nullptr;  // tile, bc, node-chunk prefix sums, (n+1) each
+  int *d_prefix = nullptr;  // tile, bc, node-chunk, indicator-run prefix sums, (n+1) each
+  int ind_items = 0;        // indicator runs in all
   unsigned *d_counters = nullptr;
   int counter_steps = 0;
+  unsigned *d_ind_counter = nullptr;  // the batched indicator's work counter
   unsigned *d_barrier = nullptr;
-  int *d_flags = nullptr;  // [0] barrier gave up, [1..2] status
+  int *d_flags = nullptr;  // [0] barrier gave up, [1..2] status, [3] indicator wait gave up
   BatchMemberStatus *d_gather = nullptr;
   // host mirrors (pinned)
   int *h_flags = nullptr;
   BatchMemberStatus *h_gather = nullptr;
   // configuration
   int tile_i = 15, blocks_per_sm = 0, steps_setting = 0, steps_per_launch = 1, grid = 0;
+  // learned form: (indicator, interval steps) pairs per graph replay, and the
+  // members' indicator settings the work plan was made with
+  int chunks = 1;
+  std::vector<std::pair<const void *, float>> ind_plan;
   cudaGraphExec_t graph = nullptr;
   bool graph_tried = false;  // capture attempted for the current configuration
   long long cells = 0, launches = 0;
@@ -76,6 +94,7 @@ BatchArgs make_args(const wenofd_batch *b, int nsteps) {
   a.work.tile_prefix = b->d_prefix;
   a.work.bc_prefix = b->d_prefix + (b->n + 1);
   a.work.pt_prefix = b->d_prefix + 2 * (b->n + 1);
+  a.work.ind_prefix = b->d_prefix + 3 * (b->n + 1);
   a.n = b->n;
   a.nsteps = nsteps;
   a.rk = b->rk;
@@ -90,21 +109,64 @@ BatchArgs make_args(const wenofd_batch *b, int nsteps) {
 // With a.members null: sets the kernel's attributes and returns its grid
 // (outside any capture); else launches on the configured grid.
 cudaError_t launch_kernel(const wenofd_batch *b, const BatchArgs &a, int *grid) {
-  return b->precision == WENOFD_FP64 ? wenofd::launch_batch_fp64(a, b->scheme, b->tile_i, b->blocks_per_sm, b->stream, grid)
-                                     : wenofd::launch_batch_fp32(a, b->scheme, b->tile_i, b->blocks_per_sm, b->stream, grid);
+  if (b->precision == WENOFD_FP64)
+    return wenofd::launch_batch_fp64(a, b->scheme, b->tile_i, b->blocks_per_sm, b->stream, grid);
+  if (b->learned) return wenofd::launch_batch_learned(a, b->scheme, b->tile_i, b->blocks_per_sm, b->stream, grid);
+  return wenofd::launch_batch_fp32(a, b->scheme, b->tile_i, b->blocks_per_sm, b->stream, grid);
 }
 
 // One launch of nsteps steps: zero the work counters and the barrier's
-// arrival count, then the cooperative kernel.
-int enqueue_launch(wenofd_batch *b, int nsteps) {
-  BATCH_TRY(cudaMemsetAsync(b->d_counters, 0, size_t(nsteps) * wenofd::kBatchPhases * sizeof(unsigned), b->stream));
+// arrival count, then the cooperative kernel.  fill_end: the launch ends
+// with the ghost fill of U^n (learned form), which takes the counters of
+// one more step.
+int enqueue_launch(wenofd_batch *b, int nsteps, bool fill_end = false) {
+  const int counted = nsteps + (fill_end ? 1 : 0);
+  BATCH_TRY(cudaMemsetAsync(b->d_counters, 0, size_t(counted) * wenofd::kBatchPhases * sizeof(unsigned), b->stream));
   BATCH_TRY(cudaMemsetAsync(b->d_barrier, 0, sizeof(unsigned), b->stream));
   int grid = b->grid;
-  BATCH_TRY(launch_kernel(b, make_args(b, nsteps), &grid));
+  BatchArgs a = make_args(b, nsteps);
+  a.fill_end = fill_end ? 1 : 0;
+  BATCH_TRY(launch_kernel(b, a, &grid));
   return WENOFD_OK;
 }
 
+// Learned form: the batched indicator over every member that can step.
+int enqueue_indicator(wenofd_batch *b) {
+  BATCH_TRY(cudaMemsetAsync(b->d_ind_counter, 0, sizeof(unsigned), b->stream));
+  BATCH_TRY(wenofd::launch_indicator_batch(b->d_members, b->d_prefix + 3 * (b->n + 1), b->n, b->d_ind_counter,
+                                           b->d_flags + 3, wenofd::guard_record(), std::max(1, b->ind_items),
+                                           b->stream));
+  return WENOFD_OK;
+}
+
+// Learned form: the launch of no steps that opens an advance (gate, then the
+// ghost fill of U^n for the first indicator run).
+int enqueue_prologue(wenofd_batch *b) { return enqueue_launch(b, 0, true); }
+
+// Learned form: `chunks` pairs of (indicator, `interval` steps).
+int enqueue_chunks(wenofd_batch *b, int chunks, int last_steps = 0) {
+  for (int k = 0; k < chunks; ++k) {
+    if (int rc = enqueue_indicator(b)) return rc;
+    const int steps = (k == chunks - 1 && last_steps > 0) ? last_steps : b->interval;
+    if (int rc = enqueue_launch(b, steps, true)) return rc;
+  }
+  return WENOFD_OK;
+}
+
+// nsteps steps of every member as the batch runs them: one launch, or for
+// the learned form the prologue and indicator/step pairs.
+int enqueue_run(wenofd_batch *b, int nsteps) {
+  if (!b->learned) return enqueue_launch(b, nsteps);
+  if (int rc = enqueue_prologue(b)) return rc;
+  const int chunks = (nsteps + b->interval - 1) / b->interval;
+  const int rem = nsteps - (chunks - 1) * b->interval;
+  return enqueue_chunks(b, chunks, rem);
+}
+
+// Work counters for launches of up to nsteps steps (and the end-of-launch
+// ghost fill of the learned form).
 int ensure_counters(wenofd_batch *b, int nsteps) {
+  nsteps += 1;
   if (nsteps <= b->counter_steps) return WENOFD_OK;
   if (b->d_counters) cudaFree(b->d_counters);
   b->d_counters = nullptr;
@@ -125,8 +187,9 @@ void drop_graph(wenofd_batch *b) {
 int plan(wenofd_batch *b, int tile_i) {
   const int TI = tile_i == 0 ? 15 : tile_i;
   std::vector<BatchMember> host(b->n);
-  std::vector<int> prefix(3 * size_t(b->n + 1), 0);
-  int *tp = prefix.data(), *bp = tp + (b->n + 1), *pp = bp + (b->n + 1);
+  std::vector<int> prefix(4 * size_t(b->n + 1), 0);
+  int *tp = prefix.data(), *bp = tp + (b->n + 1), *pp = bp + (b->n + 1), *ip = pp + (b->n + 1);
+  b->ind_plan.assign(b->n, {nullptr, 0.0f});
   for (int m = 0; m < b->n; ++m) {
     const wenofd_solver *s = b->members[m];
     BatchMember &M = host[m];
@@ -137,15 +200,27 @@ int plan(wenofd_batch *b, int tile_i) {
     M.special = s->special;
     M.ctrl = s->ctrl;
     M.tiles_j = int(ceil_div(s->ny, 32));
+    // learned form: indicator tiles are 4 x 32 nodes; each strip of them is
+    // cut into bands of about kIndBandTiles tiles
+    const bool ind = b->learned && s->ind_ready;
+    M.flags = b->learned ? s->flags : nullptr;
+    M.ind_weights = ind ? s->ind_weights : nullptr;
+    M.ind_logit_threshold = s->ind_logit_threshold;
+    M.ind_bands = int(ceil_div(ceil_div(s->nx, 4), wenofd::kIndBandTiles));
+    b->ind_plan[m] = {M.ind_weights, M.ind_logit_threshold};
     const long long tiles = ceil_div(s->nx, TI) * M.tiles_j;
     const long long bc = ceil_div(8LL * s->nx + 8LL * s->ny + 64, wenofd::kBcChunk);  // ghost entries
     const long long pts = ceil_div((long long)s->nx * s->ny, wenofd::kPtChunk);
-    if (tp[m] + tiles > 0x7fffffffLL || bp[m] + bc > 0x7fffffffLL || pp[m] + pts > 0x7fffffffLL)
+    const long long runs = b->learned ? (long long)M.ind_bands * M.tiles_j : 0;
+    if (tp[m] + tiles > 0x7fffffffLL || bp[m] + bc > 0x7fffffffLL || pp[m] + pts > 0x7fffffffLL ||
+        ip[m] + runs > 0x7fffffffLL)
       return fail(WENOFD_BAD_ARG, "batch too large: more than 2^31 work items in a phase");
     tp[m + 1] = int(tp[m] + tiles);
     bp[m + 1] = int(bp[m] + bc);
     pp[m + 1] = int(pp[m] + pts);
+    ip[m + 1] = int(ip[m] + runs);
   }
+  b->ind_items = ip[b->n];
   BATCH_TRY(cudaMemcpyAsync(b->d_members, host.data(), host.size() * sizeof(BatchMember), cudaMemcpyHostToDevice,
                             b->stream));
   BATCH_TRY(cudaMemcpyAsync(b->d_prefix, prefix.data(), prefix.size() * sizeof(int), cudaMemcpyHostToDevice,
@@ -169,17 +244,21 @@ int configure(wenofd_batch *b, int tile_i, int blocks_per_sm, int steps_per_laun
   b->steps_per_launch = steps_per_launch > 0
                             ? steps_per_launch
                             : int(std::max(1LL, std::min(64LL, (4LL << 20) / std::max(1LL, b->cells))));
+  // learned form: a graph replay runs whole (indicator, interval steps) pairs
+  b->chunks = b->learned ? std::max(1, (b->steps_per_launch + b->interval - 1) / b->interval) : 1;
+  if (b->learned) b->steps_per_launch = b->chunks * b->interval;
   if (int rc = plan(b, b->tile_i)) return rc;
-  if (int rc = ensure_counters(b, b->steps_per_launch)) return rc;
+  if (int rc = ensure_counters(b, b->learned ? b->interval : b->steps_per_launch)) return rc;
   BatchArgs q{};
   b->grid = 0;
   BATCH_TRY(launch_kernel(b, q, &b->grid));  // attributes + grid (members null)
   return WENOFD_OK;
 }
 
-// Capture one launch of steps_per_launch steps in a graph.  If the driver
-// cannot capture a cooperative launch the batch launches directly instead
-// (graph = 0 in wenofd_batch_info); the kernel is the same.
+// Capture one launch of steps_per_launch steps in a graph (learned form: its
+// indicator/step pairs).  If the driver cannot capture a cooperative launch
+// the batch launches directly instead (graph = 0 in wenofd_batch_info); the
+// kernels are the same.
 int ensure_graph(wenofd_batch *b) {
   if (b->graph_tried) return WENOFD_OK;
   b->graph_tried = true;
@@ -189,7 +268,7 @@ int ensure_graph(wenofd_batch *b) {
   b->stream = cap;
   cudaGraph_t g = nullptr;
   bool ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-  int rc = ok ? enqueue_launch(b, b->steps_per_launch) : WENOFD_OK;
+  int rc = ok ? (b->learned ? enqueue_chunks(b, b->chunks) : enqueue_launch(b, b->steps_per_launch)) : WENOFD_OK;
   if (ok) ok = cudaStreamEndCapture(cap, &g) == cudaSuccess && rc == WENOFD_OK;
   b->stream = keep;
   cudaStreamDestroy(cap);
@@ -206,11 +285,23 @@ int ensure_graph(wenofd_batch *b) {
 int launch_step_block(wenofd_batch *b) {
   if (b->graph) {
     BATCH_TRY(cudaGraphLaunch(b->graph, b->stream));
-  } else if (int rc = enqueue_launch(b, b->steps_per_launch)) {
+  } else if (int rc = b->learned ? enqueue_chunks(b, b->chunks) : enqueue_launch(b, b->steps_per_launch)) {
     return rc;
   }
-  b->launches += 1;
+  b->launches += b->learned ? 2 * b->chunks : 1;
   return WENOFD_OK;
+}
+
+// Learned form: the members' indicator weights or thresholds changed since
+// the work plan was made (wenofd_set_indicator on a member).
+bool indicator_plan_stale(const wenofd_batch *b) {
+  if (!b->learned) return false;
+  for (int m = 0; m < b->n; ++m) {
+    const wenofd_solver *s = b->members[m];
+    const void *w = s->ind_ready ? s->ind_weights : nullptr;
+    if (b->ind_plan[m].first != w || b->ind_plan[m].second != s->ind_logit_threshold) return true;
+  }
+  return false;
 }
 
 int gather(wenofd_batch *b) {
@@ -234,6 +325,7 @@ void release(wenofd_batch *b) {
   cudaFree(b->d_members);
   cudaFree(b->d_prefix);
   cudaFree(b->d_counters);
+  cudaFree(b->d_ind_counter);
   cudaFree(b->d_barrier);
   cudaFree(b->d_flags);
   cudaFree(b->d_gather);
@@ -255,12 +347,12 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
   for (int m = 0; m < n; ++m) {
     const wenofd_solver *s = members[m];
     if (!s) return fail(WENOFD_BAD_ARG, "null member handle at index " + std::to_string(m));
-    if (s->precision == WENOFD_LEARNED)
-      return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + ": the learned form is not batched");
     if (s->precision != members[0]->precision || s->scheme != members[0]->scheme || s->rk != members[0]->rk ||
         s->device != members[0]->device)
       return fail(WENOFD_BAD_ARG,
                   "member " + std::to_string(m) + ": PRECISION, SCHEME, RKMETH and DEVICE must match member 0");
+    if (s->precision == WENOFD_LEARNED && s->ind_interval != members[0]->ind_interval)
+      return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + ": INDICATOR_INTERVAL must match member 0");
     for (int k = 0; k < m; ++k)
       if (members[k] == s) return fail(WENOFD_BAD_ARG, "member " + std::to_string(m) + " repeats member " + std::to_string(k));
   }
@@ -270,6 +362,8 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
   b->precision = members[0]->precision;
   b->scheme = members[0]->scheme;
   b->rk = members[0]->rk;
+  b->learned = b->precision == WENOFD_LEARNED;
+  b->interval = b->learned ? members[0]->ind_interval : 1;
   b->members.assign(members, members + n);
   for (const wenofd_solver *s : b->members) b->cells += (long long)s->nx * s->ny;
   auto bail = [&](int rc) {
@@ -281,7 +375,8 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
     return bail(fail(WENOFD_CUDA_ERROR, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
   bool ok = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) == cudaSuccess &&
             cudaMalloc(&b->d_members, size_t(n) * sizeof(BatchMember)) == cudaSuccess &&
-            cudaMalloc(&b->d_prefix, 3 * size_t(n + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_prefix, 4 * size_t(n + 1) * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_ind_counter, sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc(&b->d_barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc(&b->d_flags, 4 * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&b->d_gather, size_t(n) * sizeof(BatchMemberStatus)) == cudaSuccess &&
@@ -329,11 +424,17 @@ int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_
   if (!b) return fail(WENOFD_BAD_ARG, "null batch handle");
   BATCH_TRY(cudaSetDevice(b->device));
   if (int rc = sync_members(b)) return rc;
+  if (indicator_plan_stale(b))
+    if (int rc = plan(b, b->tile_i)) return rc;
   if (int rc = ensure_graph(b)) return rc;
   BATCH_TRY(cudaMemsetAsync(b->d_flags, 0, 4 * sizeof(int), b->stream));
   BATCH_TRY(wenofd::launch_batch_setup(b->d_members, b->n, max_steps, b->stream));
   b->launches += 1;
   if (int rc = gather(b)) return rc;
+  if (b->learned) {
+    if (int rc = enqueue_prologue(b)) return rc;
+    b->launches += 1;
+  }
   std::vector<long long> before(b->n);
   for (int m = 0; m < b->n; ++m) before[m] = b->h_gather[m].steps;
   bool any_error = false;
@@ -356,7 +457,7 @@ int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_
     } else if (int rc = launch_step_block(b)) {
       return rc;
     }
-    BATCH_TRY(cudaMemcpyAsync(b->h_flags, b->d_flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BATCH_TRY(cudaMemcpyAsync(b->h_flags, b->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
     BATCH_TRY(cudaStreamSynchronize(b->stream));
     if (b->h_flags[0]) {
       // arrival counts are unknown after a give-up: start the barrier afresh
@@ -364,6 +465,7 @@ int wenofd_batch_advance(wenofd_batch *b, long long max_steps, long long *steps_
       BATCH_TRY(cudaStreamSynchronize(b->stream));
       return fail(WENOFD_TIMEOUT, "batched kernel: a grid barrier wait gave up");
     }
+    if (b->h_flags[3]) return fail(WENOFD_TIMEOUT, "batched indicator: a tensor-core completion wait gave up");
     any_error = any_error || b->h_flags[2] != 0;
     if (b->h_flags[1] == 0) break;
   }
@@ -403,6 +505,8 @@ int wenofd_batch_autotune(wenofd_batch *b, int steps, double *ms_per_step) {
   if (steps < 1 || steps > 4096) return fail(WENOFD_BAD_ARG, "steps must be in [1, 4096]");
   BATCH_TRY(cudaSetDevice(b->device));
   if (int rc = sync_members(b)) return rc;
+  if (indicator_plan_stale(b))
+    if (int rc = plan(b, b->tile_i)) return rc;
   const int keep_steps = b->steps_setting;
   // snapshot of every member's U^n (with ghosts) and control block
   size_t total = 0;
@@ -447,15 +551,16 @@ int wenofd_batch_autotune(wenofd_batch *b, int steps, double *ms_per_step) {
           break;
         }
         if (pass == 1 && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = fail(WENOFD_CUDA_ERROR, "event record");
-        if (!rc) rc = enqueue_launch(b, pass == 0 ? 1 : steps);
+        if (!rc) rc = enqueue_run(b, pass == 0 ? 1 : steps);
         if (!rc && pass == 1 && cudaEventRecord(e1, b->stream) != cudaSuccess)
           rc = fail(WENOFD_CUDA_ERROR, "event record");
         b->launches += 2;
         if (!rc && cudaStreamSynchronize(b->stream) != cudaSuccess)
           rc = fail(WENOFD_CUDA_ERROR, std::string("batched kernel: ") + cudaGetErrorString(cudaGetLastError()));
-        if (!rc && cudaMemcpy(b->h_flags, b->d_flags, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess &&
-            b->h_flags[0])
-          rc = fail(WENOFD_TIMEOUT, "batched kernel: a grid barrier wait gave up");
+        if (!rc && cudaMemcpy(b->h_flags, b->d_flags, 4 * sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess &&
+            (b->h_flags[0] || b->h_flags[3]))
+          rc = fail(WENOFD_TIMEOUT, b->h_flags[0] ? "batched kernel: a grid barrier wait gave up"
+                                                  : "batched indicator: a tensor-core completion wait gave up");
         if (!rc) rc = copy_all(false);
       }
       if (!rc && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && (best_ms < 0 || ms < best_ms)) {

@@ -85,18 +85,6 @@ struct Nothing {
   __device__ void operator()() const {}
 };
 
-// Member owning work item `item` of a prefix array (n+1 entries).  The
-// prefix arrays and the member table are read-only for the whole launch.
-__device__ __forceinline__ int owner(const int *prefix, int n, int item) {
-  int lo = 0, hi = n;  // prefix[lo] <= item < prefix[hi]
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(&prefix[mid]) <= item) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
 // Hand out the items [0, prefix[n]) of one phase to the blocks.  Thread 0
 // claims an item from the phase's counter, finds its member and reads the
 // member's `active` flag; the claim of the next item is issued before the
@@ -146,7 +134,10 @@ __device__ __forceinline__ int runnable(const Ctrl *c) {
   return (!__ldcg(&c->done) && !__ldcg(&c->error) && __ldcg(&c->steps) < __ldcg(&c->max_steps)) ? 1 : 0;
 }
 
-template <typename T, int SCHEME, int TI, int NT, bool WITHHOLD = false>
+// ROUTE (FP32 only): the learned form; each member's stage tiles route
+// their faces with the member's flags (BatchMember::flags), which the
+// batched indicator launch between two launches of this kernel writes.
+template <typename T, int SCHEME, int TI, int NT, bool WITHHOLD = false, bool ROUTE = false>
 __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) k_batch(BatchArgs b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BatchMember sM;
@@ -318,9 +309,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         a.dt = &M.ctrl->dt;
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
-        a.flags = nullptr;
+        a.flags = ROUTE ? M.flags : nullptr;
         if constexpr (F32)
-          stage_tile_f32<SCHEME, TI, TJ, NT, false, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
+          stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
         else stage_tile_f64<SCHEME, TI, TJ, NT, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < nst - 1 || b.rk == 0) barrier(Nothing());
@@ -340,6 +331,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
       barrier(step_end);
     }
   }
+  // the ghost nodes of U^n for the indicator launch that follows (members
+  // that can step; `active` was set by the last gate)
+  if (b.fill_end) {
+    for_member_items(b, b.counters + b.nsteps * kBatchPhases, b.work.bc_prefix, sM,
+                     [&](int local, const BatchMember &M) {
+                       const int first = local * kBcChunk, total = bc_entries(M.g);
+                       for (int e = first + int(threadIdx.x); e < first + kBcChunk && e < total; e += NT)
+                         bc_fill_entry(M.g, M.S, M.special, e);
+                     });
+  }
 }
 
 // Cooperative launch of one kernel instance.  With b.members null: sets the
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
 // resident blocks per SM (occupancy, or blocks_per_sm if smaller); call it
 // outside stream capture.  Otherwise launches *grid blocks, which must come
 // from that query.
-template <typename T, int TI, int NT, bool WITHHOLD = false>
+template <typename T, int TI, int NT, bool WITHHOLD = false, bool ROUTE = false>
 cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm, cudaStream_t s, int *grid) {
   constexpr size_t smem = stage_smem_bytes<T, TI, 32, false, NT>();
   void (*fn)(BatchArgs) = nullptr;
@@ -356,10 +357,10 @@ cudaError_t launch_batch_tile(const BatchArgs &b, int scheme, int blocks_per_sm,
     fn = k_batch<T, kWenoZ, TI, NT, true>;
   } else {
     switch (scheme) {
-      case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT>; break;
-      case kWenoZ: fn = k_batch<T, kWenoZ, TI, NT>; break;
-      case kWenoZP: fn = k_batch<T, kWenoZP, TI, NT>; break;
-      case kWenoZPI: fn = k_batch<T, kWenoZPI, TI, NT>; break;
+      case kWenoJS: fn = k_batch<T, kWenoJS, TI, NT, false, ROUTE>; break;
+      case kWenoZ: fn = k_batch<T, kWenoZ, TI, NT, false, ROUTE>; break;
+      case kWenoZP: fn = k_batch<T, kWenoZP, TI, NT, false, ROUTE>; break;
+      case kWenoZPI: fn = k_batch<T, kWenoZPI, TI, NT, false, ROUTE>; break;
       default: return cudaErrorInvalidValue;
     }
   }

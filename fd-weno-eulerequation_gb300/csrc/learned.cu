@@ -18,6 +18,7 @@
 
 #include "../../include/wenofd.h"
 
+#include "aux_device.cuh"
 #include "guard.cuh"
 #include "learned_common.cuh"
 #include "trace.h"
@@ -390,75 +391,55 @@ __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A
 
 constexpr int kResident = 8;  // CTAs per SM: 28 KB shared memory, 64 registers, 64 TMEM columns each
 
-__global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
-                                                            float logit_threshold, unsigned char *flags,
-                                                            int flag_pitch, int *error, const int *active,
-                                                            const Ctrl *ctrl, int interval) {
-  if (active && *active == 0) return;
-  if (ctrl && interval > 1 && (ctrl->steps - ctrl->ind_base) % interval != 0) return;
-  __shared__ __align__(128) __nv_bfloat16 sA[kCells * kK1];  // A1, then A2 [128 x 48] (and the layer-3 input)
-  __nv_bfloat16 *const sA1 = sA, *const sA2 = sA;
-  __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
-  __shared__ __align__(128) __nv_bfloat16 sB2[kHid * kK2];
-  __shared__ __align__(128) __nv_bfloat16 sB3[kN3 * kK2];
-  __shared__ float sRho[kPI * kPJ], sPre[kPI * kPJ];
-  __shared__ __align__(8) unsigned long long mbar;
-  __shared__ unsigned tmem_base_sh;
+// Shared memory of one indicator CTA: the BF16 operands and the node patch.
+struct IndSmem {
+  __nv_bfloat16 *A;                 // A1, then A2 [128 x 48] (and the layer-3 input)
+  const __nv_bfloat16 *B1, *B2, *B3;  // the layers' weights
+  float *rho, *pre;                 // the node patch ring
+};
 
+// Per-CTA tensor-core state: TMEM columns, the completion mbarrier and its
+// phase, and whether a wait gave up.
+struct IndTc {
+  unsigned tmem, mb, parity;
+  bool failed;
+};
+
+// One band of indicator tiles: tiles first .. last-1 (4 rows x 32 columns of
+// cells each) down strip `strip` of the grid g, state U (ghosts filled),
+// flags written at flags[(kGhost + i) * flag_pitch + kGhost + j].  Every
+// thread of the CTA calls it.  The node patch is a ring of 8 rows, node row
+// i in slot i & 7: consecutive tiles of a band share 4 of their 8 patch
+// rows, so every tile after the band's first loads 4 rows.  Returns false
+// when a tensor-core wait gave up (recorded in *error); the CTA then stops.
+__device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, float logit_threshold,
+                                               unsigned char *flags, int flag_pitch, int *error, int strip, int first,
+                                               int last, const IndSmem &sm, IndTc &tc) {
   const int tid = threadIdx.x, warp = tid >> 5;
-  for (int k = tid; k < kHid * kK1; k += kCells) sB1[k] = W->w1[k];
-  for (int k = tid; k < kHid * kK2; k += kCells) sB2[k] = W->w2[k];
-  for (int k = tid; k < kN3 * kK2; k += kCells) sB3[k] = W->w3[k];
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&tmem_base_sh)));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  fence_async_smem();
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const unsigned tmem = tmem_base_sh;
-  const unsigned mb = smem_u32(&mbar);
   const unsigned lane_base = unsigned(32 * warp) << 16;
   const float gam = float(g.gamma);
-  // CTA b walks one band of rows down one strip (a strip = 32 columns, tiles
-  // of 4 rows each): strip b % tiles_j, band b / tiles_j of the grid's
-  // gridDim.x / tiles_j bands.  CTAs of neighbouring strips and the same band
-  // start at the same row and move down together, so the patch columns they
-  // share are read from L2 while both need them.  The node patch is a ring
-  // of 8 rows, node row i in slot i & 7: consecutive tiles of a strip share 4
-  // of their 8 patch rows, so every tile after a band's first loads 4 rows.
-  const int tiles_i = (g.nx + kTileI - 1) / kTileI;
-  const int tiles_j = (g.ny + kTileJ - 1) / kTileJ;
-  const int bands = int(gridDim.x) / tiles_j;
-  const int strip = int(blockIdx.x) % tiles_j, band = int(blockIdx.x) / tiles_j;
-  const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
+  __nv_bfloat16 *const sA1 = sm.A, *const sA2 = sm.A;
+  float *const sRho = sm.rho, *const sPre = sm.pre;
   static_assert(kPI == 2 * kTileI, "ring of two tiles' rows");
-  unsigned parity = 0;
 
   // One layer: barrier (the operand writes are visible to the tensor core),
   // MMA issue by thread 0, completion wait by every thread.  A wait that
   // gives up marks this thread failed; the next barrier (a vote) turns that
   // into a uniform stop of the whole CTA.
-  bool failed = false;
   auto layer = [&](auto issue) -> bool {
     fence_async_smem();
     tc_fence_before();
-    if (__syncthreads_or(failed)) return false;
+    if (__syncthreads_or(tc.failed)) return false;
     if (tid == 0) {
       tc_fence_after();
       issue();
-      mma_commit(mb);
+      mma_commit(tc.mb);
     }
-    if (!mbar_wait(mb, parity)) {
-      failed = true;
+    if (!mbar_wait(tc.mb, tc.parity)) {
+      tc.failed = true;
       atomicExch(error, 1);
     }
-    parity ^= 1u;
+    tc.parity ^= 1u;
     tc_fence_after();
     return true;
   };
@@ -520,38 +501,171 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
       window_store(w, sA1, tid, kColP, 0.0f, 0.0f, g.guard);
     }
     // 3. layer 1 (bias included)
-    if (!layer([&] { mma_layer<kK1, kHid>(tmem, sA1, sB1); })) break;
+    if (!layer([&] { mma_layer<kK1, kHid>(tc.tmem, sA1, sm.B1); })) return false;
     // 4. GELU -> A2
     {
       float z[32];
-      tmem_ld32(tmem + lane_base, z);
+      tmem_ld32(tc.tmem + lane_base, z);
       gelu_row_store(z, sA2, tid, g.guard);
     }
     // 5. layer 2
-    if (!layer([&] { mma_layer<kK2, kHid>(tmem + 32, sA2, sB2); })) break;
+    if (!layer([&] { mma_layer<kK2, kHid>(tc.tmem + 32, sA2, sm.B2); })) return false;
     // 6. GELU -> A2 (layer 2 has read it)
     {
       float z[32];
-      tmem_ld32(tmem + lane_base + 32, z);
+      tmem_ld32(tc.tmem + lane_base + 32, z);
       gelu_row_store(z, sA2, tid, g.guard);
     }
     // 7. output layer on the tensor cores, into the columns of D1
-    if (!layer([&] { mma_layer<kK2, kN3>(tmem, sA2, sB3); })) break;
+    if (!layer([&] { mma_layer<kK2, kN3>(tc.tmem, sA2, sm.B3); })) return false;
     {
       float d[2];
-      tmem_ld2(tmem + lane_base, d);
+      tmem_ld2(tc.tmem + lane_base, d);
       const float logit = d[0] + d[1];
       const int i = i0 + warp, j = j0 + (tid & 31);
-      if (i < g.nx && j < g.ny && !failed)
+      if (i < g.nx && j < g.ny && !tc.failed)
         flags[WENOFD_IX(g.guard, (long long)(kGhost + i) * flag_pitch + (kGhost + j), (long long)g.nxt * flag_pitch)] =
             logit > logit_threshold ? 1 : 0;
     }
     tc_fence_before();
-    if (__syncthreads_or(failed)) break;
+    if (__syncthreads_or(tc.failed)) return false;
   }
+  return true;
+}
+
+// Copies the packed weights into the CTA's operand buffers (all threads).
+__device__ __forceinline__ void load_weights(const IndicatorWeights *W, __nv_bfloat16 *B1, __nv_bfloat16 *B2,
+                                             __nv_bfloat16 *B3) {
+  for (int k = threadIdx.x; k < kHid * kK1; k += kCells) B1[k] = W->w1[k];
+  for (int k = threadIdx.x; k < kHid * kK2; k += kCells) B2[k] = W->w2[k];
+  for (int k = threadIdx.x; k < kN3 * kK2; k += kCells) B3[k] = W->w3[k];
+}
+
+// CTA set-up: the completion mbarrier and 64 tensor-memory columns.
+__device__ __forceinline__ IndTc indicator_open(unsigned long long *mbar, unsigned *tmem_base_sh) {
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((threadIdx.x >> 5) == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(tmem_base_sh)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  IndTc tc;
+  tc.tmem = *tmem_base_sh;
+  tc.mb = smem_u32(mbar);
+  tc.parity = 0;
+  tc.failed = false;
+  return tc;
+}
+
+// CTA tear-down: the tensor memory is released (after every MMA completed
+// or the CTA stopped).
+__device__ __forceinline__ void indicator_close(const IndTc &tc) {
   tc_fence_after();
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+  if ((threadIdx.x >> 5) == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tc.tmem));
+}
+
+__global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
+                                                            float logit_threshold, unsigned char *flags,
+                                                            int flag_pitch, int *error, const int *active,
+                                                            const Ctrl *ctrl, int interval) {
+  if (active && *active == 0) return;
+  if (ctrl && interval > 1 && (ctrl->steps - ctrl->ind_base) % interval != 0) return;
+  __shared__ __align__(128) __nv_bfloat16 sA[kCells * kK1];
+  __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
+  __shared__ __align__(128) __nv_bfloat16 sB2[kHid * kK2];
+  __shared__ __align__(128) __nv_bfloat16 sB3[kN3 * kK2];
+  __shared__ float sRho[kPI * kPJ], sPre[kPI * kPJ];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ unsigned tmem_base_sh;
+
+  load_weights(W, sB1, sB2, sB3);
+  IndTc tc = indicator_open(&mbar, &tmem_base_sh);
+  // CTA b walks one band of rows down one strip (a strip = 32 columns, tiles
+  // of 4 rows each): strip b % tiles_j, band b / tiles_j of the grid's
+  // gridDim.x / tiles_j bands.  CTAs of neighbouring strips and the same band
+  // start at the same row and move down together, so the patch columns they
+  // share are read from L2 while both need them.
+  const int tiles_i = (g.nx + kTileI - 1) / kTileI;
+  const int tiles_j = (g.ny + kTileJ - 1) / kTileJ;
+  const int bands = int(gridDim.x) / tiles_j;
+  const int strip = int(blockIdx.x) % tiles_j, band = int(blockIdx.x) / tiles_j;
+  const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
+  const IndSmem sm{sA, sB1, sB2, sB3, sRho, sPre};
+  indicator_band(g, U, logit_threshold, flags, flag_pitch, error, strip, first, last, sm, tc);
+  indicator_close(tc);
+}
+
+// The indicator runs of a learned batch (launch_indicator_batch).  Work item
+// = (member, strip, band): the member from the prefix array, then strip =
+// local % tiles_j and band = local / tiles_j of the member's ind_bands bands
+// (its tiles split evenly among them).  A CTA claims items from *counter
+// until none is left, skips members that cannot step or have no weights,
+// and reloads the weights only when the member's weights differ from the
+// ones it holds.
+__global__ void __launch_bounds__(kCells, kResident)
+    k_indicator_batch(const BatchMember *members, const int *prefix, int n, unsigned *counter, int *error,
+                      unsigned long long *guard) {
+  __shared__ __align__(128) __nv_bfloat16 sA[kCells * kK1];
+  __shared__ __align__(128) __nv_bfloat16 sB1[kHid * kK1];
+  __shared__ __align__(128) __nv_bfloat16 sB2[kHid * kK2];
+  __shared__ __align__(128) __nv_bfloat16 sB3[kN3 * kK2];
+  __shared__ float sRho[kPI * kPJ], sPre[kPI * kPJ];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ unsigned tmem_base_sh;
+  __shared__ int s_item, s_m, s_on;
+  __shared__ BatchMember sM;  // the record of the member whose items run
+
+  IndTc tc = indicator_open(&mbar, &tmem_base_sh);
+  const IndSmem sm{sA, sB1, sB2, sB3, sRho, sPre};
+  const int total = __ldg(&prefix[n]);
+  int cur = -1;                  // member staged in sM
+  const void *loaded = nullptr;  // weights now in sB1..sB3
+  for (;;) {
+    __syncthreads();  // every thread has read the last claim and sM
+    if (threadIdx.x == 0) {
+      const int item = int(atomicAdd(counter, 1u));
+      s_item = item;
+      if (item < total) {
+        const int m = WENOFD_IX(guard, dev::owner(prefix, n, item), n);
+        s_m = m;
+        const BatchMember *M = members + m;
+        s_on = M->ind_weights != nullptr && *(volatile const int *)&M->ctrl->active != 0;
+      }
+    }
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) break;
+    if (!s_on) continue;  // block-uniform: the member cannot step or has no weights
+    const int m = s_m;
+    if (m != cur) {  // block-uniform: stage the member record
+      const unsigned *src = reinterpret_cast<const unsigned *>(members + m);
+      unsigned *dst = reinterpret_cast<unsigned *>(&sM);
+      for (int w = threadIdx.x; w < int(sizeof(BatchMember) / 4); w += kCells) dst[w] = __ldg(&src[w]);
+      __syncthreads();
+      cur = m;
+      if (sM.ind_weights != loaded) {
+        // every MMA that read the old weights has completed (each layer waits)
+        load_weights(static_cast<const IndicatorWeights *>(sM.ind_weights), sB1, sB2, sB3);
+        loaded = sM.ind_weights;
+      }
+    }
+    const Geom &g = sM.g;
+    const int tiles_i = (g.nx + kTileI - 1) / kTileI;
+    const int tiles_j = (g.ny + kTileJ - 1) / kTileJ;
+    const int bands = sM.ind_bands;
+    const int local = item - __ldg(&prefix[m]);
+    const int strip = local % tiles_j, band = local / tiles_j;
+    const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
+    if (!indicator_band(g, sM.S, sM.ind_logit_threshold, sM.flags, g.pitch, error, strip, first, last, sm, tc)) break;
+  }
+  indicator_close(tc);
 }
 
 }  // namespace lrn
@@ -624,6 +738,20 @@ cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights
   lrn::k_indicator_tc<<<grid, lrn::kCells, 0, s>>>(g, U, static_cast<const lrn::IndicatorWeights *>(weights),
                                                    logit_threshold, flags, g.pitch, error, active, ctrl,
                                                    interval);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_indicator_batch(const BatchMember *members, const int *ind_prefix, int n, unsigned *counter,
+                                   int *error, unsigned long long *guard, int items, cudaStream_t s) {
+  static int sms_of[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int &sms = sms_of[dev & 63];
+  if (sms == 0 && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  // every CTA resident at once; no more CTAs than work items
+  const int grid = std::max(1, std::min(items, sms * lrn::kResident));
+  lrn::k_indicator_batch<<<grid, lrn::kCells, 0, s>>>(members, ind_prefix, n, counter, error, guard);
   return cudaGetLastError();
 }
 

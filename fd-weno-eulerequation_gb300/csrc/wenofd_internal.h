@@ -139,6 +139,14 @@ struct BatchMember {
   const double *special;
   Ctrl *ctrl;
   int tiles_j;  // tiles along y; tiles along x = ceil(nx / TI)
+  // Learned form: the member's routing flags ([nxt][pitch], ghosts 1) and
+  // packed indicator weights (null: no indicator loaded, the flags stay as
+  // they are), its logit threshold, and the bands of indicator tiles per
+  // strip (indicator work items = strips x bands).
+  unsigned char *flags;
+  const void *ind_weights;
+  float ind_logit_threshold;
+  int ind_bands;
 };
 
 // Exclusive prefix sums of work items per member (n+1 entries each).
@@ -146,6 +154,7 @@ struct BatchWork {
   const int *tile_prefix;  // stage tiles (depends on TI)
   const int *bc_prefix;    // ghost-fill chunks of kBcChunk entries
   const int *pt_prefix;    // time-step chunks of kPtChunk nodes
+  const int *ind_prefix;   // learned form: indicator runs (strip, band of rows)
 };
 
 constexpr int kBcChunk = 256;
@@ -165,6 +174,12 @@ struct BatchArgs {
   unsigned *barrier;   // [0] arrivals (zero before the launch), [1] generation
   int *error;          // set if a barrier wait gave up
   int *status;         // after the launch: [0] members that can still step, [1] any member error
+  // After the launch's last step, fill the ghost nodes of every member that
+  // can still step (its U^n, S): the learned form's indicator, launched
+  // between two batched launches, reads the next step's stage-1 input with
+  // its ghosts, as the single solve's indicator does.  Uses the counters of
+  // step nsteps (the counter array then holds nsteps + 1 steps).
+  int fill_end = 0;
   // Test instance only (k_batch with WITHHOLD): block `hold_block` skips its
   // arrival at the launch's barrier number `hold_barrier` (counted from 0).
   int hold_block = -1, hold_barrier = -1;
@@ -183,6 +198,10 @@ cudaError_t launch_batch_fp64(const BatchArgs &b, int scheme, int tile_i, int bl
                               int *grid);
 cudaError_t launch_batch_fp32(const BatchArgs &b, int scheme, int tile_i, int blocks_per_sm, cudaStream_t s,
                               int *grid);
+// batch_learned.cu: the FP32 batched kernel with routed stage tiles (the
+// learned form; members' flags route each face).
+cudaError_t launch_batch_learned(const BatchArgs &b, int scheme, int tile_i, int blocks_per_sm, cudaStream_t s,
+                                 int *grid);
 // The FP64 WENO-Z batched kernel (tile 15) built with the withholding test
 // hook and a short barrier poll limit: exercises the barrier's give-up path.
 // Never launched by wenofd_batch_advance unless wenofd_batch_test_withhold
@@ -219,6 +238,16 @@ cudaError_t launch_sample_write(const Geom &g, const double *U, const unsigned c
 cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
                              unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
                              cudaStream_t s);
+// Indicator runs of a learned batch: one launch over every member that can
+// step and has weights loaded (BatchMember::ind_weights), on its U^n (ghosts
+// filled), into its flags.  Work items are (member, strip, band of rows) from
+// ind_prefix, claimed through *counter (zeroed before the launch).  The
+// tiles and arithmetic are the single solve's, so the flags are too.
+// `items` = ind_prefix[n] (the grid is no larger).
+cudaError_t launch_indicator_batch(const BatchMember *members, const int *ind_prefix, int n, unsigned *counter,
+                                   int *error, unsigned long long *guard, int items, cudaStream_t s);
+// Rows of 4-node indicator tiles per batched indicator work item.
+constexpr int kIndBandTiles = 16;
 
 // aux_kernels.cu
 cudaError_t launch_bc_fill(const Geom &g, double *U, const double *special, const int *active, cudaStream_t s);

@@ -241,18 +241,27 @@ int wenofd_mlp_init(float *host_params, unsigned long long seed);
  * by one kernel launch per few steps that advances every member.
  *
  * Members are existing handles: same device, same SCHEME, same RKMETH (RK1,
- * SSP-RK2 or SSP-RK3) and the same PRECISION, FP64 or FP32 (the learned
- * form is not batched); sizes, test cases, boundary conditions, CFL and TEND
- * may differ.  The
+ * SSP-RK2 or SSP-RK3) and the same PRECISION (FP64, FP32 or LEARNED; learned
+ * members also the same INDICATOR_INTERVAL); sizes, test cases, boundary
+ * conditions, CFL, TEND and the learned members' indicator weights and
+ * thresholds may differ.  The
  * batch works on the members' own device state: a member stepped by a
- * batch is read (wenofd_get_state, wenofd_get_info, ...) through its own
- * handle; members must outlive the batch and must not be advanced through
- * their own handles while a batch call runs.  Each member's steps are
- * those of wenofd_advance on its own: FP64 members bit for bit.
+ * batch is read (wenofd_get_state, wenofd_get_info, wenofd_routing_flags,
+ * ...) through its own handle; members must outlive the batch and must not
+ * be advanced through their own handles while a batch call runs.  Each
+ * member's steps are those of wenofd_advance on its own: FP64 members bit
+ * for bit.  Learned members: one tensor-core indicator launch over all of
+ * them runs on the first step of every wenofd_batch_advance call and then
+ * every INDICATOR_INTERVAL steps (between launches of the batched kernel,
+ * which routes each member's faces with its flags), as in wenofd_advance;
+ * a member without weights (no wenofd_set_indicator) routes every face to
+ * WENO.  Weights loaded on a member reach the batch's next call.
  *
- * wenofd_batch_configure: tile rows per stage tile (FP64: 7 or 15, FP32: 15
- *   or 31; 0 = default 15), resident blocks per SM (0 = as many as fit) and
- *   steps per launch (0 = chosen from the batch's size).
+ * wenofd_batch_configure: tile rows per stage tile (FP64: 7 or 15, FP32 and
+ *   learned: 15 or 31; 0 = default 15), resident blocks per SM (0 = as many
+ *   as fit) and steps per launch (0 = chosen from the batch's size; learned
+ *   batches round it up to whole INDICATOR_INTERVAL runs of steps, each its
+ *   own launch after an indicator launch).
  * wenofd_batch_autotune: times each (tile, blocks per SM) candidate over
  *   `steps` steps, keeps the fastest and returns its milliseconds per step;
  *   the members' states and times are restored after every trial.
@@ -261,7 +270,8 @@ int wenofd_mlp_init(float *host_params, unsigned long long seed);
  *   *steps_done receives the largest number of steps a member took.
  *   WENOFD_NAN_DT if a member's time step became NaN (that member stops,
  *   the others finish the call; the message names the member index);
- *   WENOFD_TIMEOUT if a grid barrier wait gave up. */
+ *   WENOFD_TIMEOUT if a grid barrier wait or a tensor-core completion wait
+ *   of the batched indicator gave up. */
 typedef struct wenofd_batch wenofd_batch;
 
 typedef struct wenofd_batch_info {
@@ -270,7 +280,7 @@ typedef struct wenofd_batch_info {
   int tile_i;            /* tile rows of the stage tiles */
   int blocks_per_sm;     /* resident blocks per SM of the persistent kernel */
   int grid;              /* blocks per launch */
-  int steps_per_launch;  /* time steps one launch runs */
+  int steps_per_launch;  /* time steps one launch (learned: one graph replay) runs */
   int graph;             /* 1: launches are replays of a captured CUDA graph */
   long long cells;       /* interior nodes over all members */
   long long launches;    /* kernels launched by this batch so far */

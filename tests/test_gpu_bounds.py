@@ -87,17 +87,25 @@ def run_all(out_path):
             if c[6] == wenofd.LEARNED:
                 out[f"c{k}_flags"] = s.indicator_flags()
                 out[f"c{k}_routing"] = s.routing_flags()
-    # batches: FP64 with RK1, SSP-RK2, SSP-RK3; one FP32 batch
+    # batches: FP64 with RK1, SSP-RK2, SSP-RK3; one FP32 batch; learned
+    # batches (the batched indicator and the routed batched kernel) with
+    # both tile heights
     members = [(4, 16, 12, 3), (3, 37, 29, 0), (1, 70, 45, 0), (0, 13, 7, 0)]
-    for rk, prec in ((0, 0), (1, 0), (2, 0), (2, 1)):
+    for rk, prec, tile in ((0, 0, 0), (1, 0, 0), (2, 0, 0), (2, 1, 0), (2, 2, 15), (1, 2, 31)):
         solvers = [wenofd.Solver(_cfg(tc, nx, ny, sd, 1, rk, prec, 0)) for tc, nx, ny, sd in members]
         try:
             for s in solvers:
                 s.initialize()
+                if prec == wenofd.LEARNED:
+                    s.set_indicator(params, 0.5)
             with wenofd.Batch(solvers) as b:
+                if tile:
+                    b.configure(tile_i=tile)
                 b.advance(STEPS)
             for m, s in enumerate(solvers):
                 out[f"b{rk}{prec}_{m}"] = s.get_state()
+                if prec == wenofd.LEARNED:
+                    out[f"bflags{rk}{prec}_{m}"] = s.routing_flags()
         finally:
             for s in solvers:
                 s.close()
@@ -144,6 +152,8 @@ def _bound(k):
         if what in ("flags", "routing"):
             return ("fraction", FLAG_FRACTION)
         return ("rel", RHS_REL_TOL if what == "rhs" else FP32_REL_TOL)
+    if k.startswith("bflags"):  # learned batch member's routing flags
+        return ("fraction", FLAG_FRACTION)
     if k.startswith("b"):  # batch b<rk><precision>_<member>
         return None if k[2] == "0" else ("rel", FP32_REL_TOL)
     if k.startswith("train"):
