@@ -249,7 +249,12 @@ def kernel_tour(wenofd, torch, device: int, n: int) -> dict:
     without allocation on its state; one FP64 WENO-JS step of the smooth wave and its
     density error norms; the learned form's data
     extraction, one training epoch on that data, and one step with the
-    trained indicator; one step of a two-member FP32 and FP64 batch."""
+    trained indicator; one step of a two-member FP32 and FP64 batch; one
+    advance of INDICATOR_INTERVAL steps of a learned batch of the batching
+    leg's 64 uneven shear layers (16 M nodes: the batched indicator once, the
+    routed batched kernel once after its opening launch)."""
+    import numpy as np
+
     from wenofd import learned
 
     ran = {}
@@ -290,6 +295,21 @@ def kernel_tour(wenofd, torch, device: int, n: int) -> dict:
             ran[name] = {"steps": b.advance(max_steps=1)}
         for s in members:
             s.close()
+    members = []
+    for k in range(BATCH_MEMBERS):
+        nx, ny = BATCH_SHAPES[k % len(BATCH_SHAPES)]
+        s = wenofd.Solver({"TESTCASE": 5, "ELEMNUMX": nx, "ELEMNUMY": ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
+                           "SEED": 1000 + k, "PRECISION": wenofd.LEARNED, "DEVICE": device,
+                           "INDICATOR_INTERVAL": INDICATOR_INTERVAL})
+        s.initialize()
+        s.set_indicator(params, THRESHOLD)
+        members.append(s)
+    with wenofd.Batch(members) as b:
+        b.configure(steps_per_launch=INDICATOR_INTERVAL)
+        ran["batch_learned"] = {"steps": b.advance(max_steps=INDICATOR_INTERVAL),
+                                "flagged": float(np.mean([m.routing_flags().mean() for m in members]))}
+    for s in members:
+        s.close()
     torch.cuda.synchronize(device)
     return ran
 
