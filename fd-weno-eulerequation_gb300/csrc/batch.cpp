@@ -47,7 +47,7 @@ struct wenofd_batch {
   int counter_steps = 0;
   unsigned *d_ind_counter = nullptr;  // the batched indicator's work counter
   unsigned *d_barrier = nullptr;
-  int *d_flags = nullptr;  // [0] barrier gave up, [1..2] status, [3] indicator wait gave up
+  int *d_flags = nullptr;  // [0] barrier gave up, [1..2] status, [3] indicator wait gave up, [4] all bounds valid
   BatchMemberStatus *d_gather = nullptr;
   // host mirrors (pinned)
   int *h_flags = nullptr;
@@ -102,6 +102,7 @@ BatchArgs make_args(const wenofd_batch *b, int nsteps) {
   a.barrier = b->d_barrier;
   a.error = b->d_flags;
   a.status = b->d_flags + 1;
+  a.all_bounds = b->d_flags + 4;
   a.guard = wenofd::guard_record();
   return a;
 }
@@ -207,6 +208,7 @@ int plan(wenofd_batch *b, int tile_i) {
     M.ind_weights = ind ? s->ind_weights : nullptr;
     M.ind_logit_threshold = s->ind_logit_threshold;
     M.ind_bands = int(ceil_div(ceil_div(s->nx, 4), wenofd::kIndBandTiles));
+    M.tile_bounds = s->tile_bounds;
     b->ind_plan[m] = {M.ind_weights, M.ind_logit_threshold};
     const long long tiles = ceil_div(s->nx, TI) * M.tiles_j;
     const long long bc = ceil_div(8LL * s->nx + 8LL * s->ny + 64, wenofd::kBcChunk);  // ghost entries
@@ -378,12 +380,12 @@ int wenofd_batch_create(wenofd_solver *const *members, int n, wenofd_batch **out
             cudaMalloc(&b->d_prefix, 4 * size_t(n + 1) * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&b->d_ind_counter, sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc(&b->d_barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
-            cudaMalloc(&b->d_flags, 4 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&b->d_flags, 8 * sizeof(int)) == cudaSuccess &&
             cudaMalloc(&b->d_gather, size_t(n) * sizeof(BatchMemberStatus)) == cudaSuccess &&
             cudaMallocHost(&b->h_flags, 4 * sizeof(int)) == cudaSuccess &&
             cudaMallocHost(&b->h_gather, size_t(n) * sizeof(BatchMemberStatus)) == cudaSuccess;
   ok = ok && cudaMemsetAsync(b->d_barrier, 0, 2 * sizeof(unsigned), b->stream) == cudaSuccess &&
-       cudaMemsetAsync(b->d_flags, 0, 4 * sizeof(int), b->stream) == cudaSuccess;
+       cudaMemsetAsync(b->d_flags, 0, 8 * sizeof(int), b->stream) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
     return bail(fail(WENOFD_CUDA_ERROR, "batch allocation failed"));

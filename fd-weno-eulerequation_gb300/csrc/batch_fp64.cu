@@ -8,7 +8,8 @@ namespace wenofd {
 namespace {
 
 // k_advance_setup of every member: the step budget of this advance call
-// and a clean reduction state.
+// and a clean reduction state (no tile bounds: the batch's tiles may differ
+// from the single solve's, so the first step screens every node).
 __global__ void k_batch_setup(BatchMember *members, int n, long long max_steps) {
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
     Ctrl *c = members[m].ctrl;
@@ -17,6 +18,7 @@ __global__ void k_batch_setup(BatchMember *members, int n, long long max_steps) 
     c->max_s_bits = 0ull;
     c->screen_bits = 0u;
     c->nan_flag = 0;
+    c->bounds_valid = 0;
   }
 }
 

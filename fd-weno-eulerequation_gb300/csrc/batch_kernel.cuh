@@ -5,6 +5,10 @@
 // sequence of phases separated by grid-wide barriers:
 //   time-step reduction (FP64 exact pass; FP32 forms: screen, then refine)
 //   -> dt of every member -> 3 x (boundary fill -> stage tiles) -> time update.
+// As in the single solve, the FP32 forms' last RK stage screens the nodes it
+// writes (per-tile bounds), so from a member's second step on its time-step
+// reduction is the exact FP64 pass over the few tiles whose bound reaches
+// the maximum lower bound, a warp per tile.
 // Inside a phase the blocks take work items (stage tiles, ghost strips, node
 // chunks) of all members from one atomic counter, so uneven member sizes
 // balance across the GPU.  The per-member control work between phases (dt,
@@ -147,12 +151,22 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
   int nbar = 0;  // barriers passed in this launch (the WITHHOLD hook's index)
   auto barrier = [&](auto last) { grid_barrier<WITHHOLD>(b, last, nbar++); };
 
-  // the loop condition of src/WENOFD.cpp:213, per member
+  // the loop condition of src/WENOFD.cpp:213, per member; FP32 forms: whether
+  // every member that can step holds valid tile bounds (BatchArgs::all_bounds)
   auto gate = [&]() {
-    for (int m = threadIdx.x; m < n; m += NT) {
-      Ctrl *c = b.members[m].ctrl;
-      c->active = runnable(c);
+    int all = 1;
+    for (int base = 0; base < n; base += NT) {
+      const int m = base + int(threadIdx.x);
+      int ok = 1;
+      if (m < n) {
+        Ctrl *c = b.members[m].ctrl;
+        const int can = runnable(c);
+        c->active = can;
+        ok = !can || __ldcg(&c->bounds_valid);
+      }
+      all &= __syncthreads_and(ok);
     }
+    if (F32 && threadIdx.x == 0) *b.all_bounds = all;
   };
   // dt = min(1, cfl / max s), clipped to t_end - now (src/WENOFD.cpp:401,
   // 426-435); NaN -> error NAN_DT (lines 437-442)
@@ -226,32 +240,96 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         if (nan_seen) atomicOr(&M.ctrl->nan_flag, 1);
       }
     };
-    if constexpr (F32) {
-      // screen: L = max (s32 - e), a lower bound of the member's max s
-      for_member_items(b, cnt + 0, b.work.pt_prefix, sM, [&](int local, const BatchMember &M) {
-        const long long first = (long long)local * kPtChunk;
-        const long long npts = (long long)M.g.nx * M.g.ny;
-        float lo = 0.0f;
-        for (long long t = first + threadIdx.x; t < first + kPtChunk && t < npts; t += NT) {
-          double rho, mu, mv, E;
-          node(M, t, rho, mu, mv, E);
-          float s, e;
-          screen_speed(M.g, rho, mu, mv, E, s, e);
-          lo = fmaxf(lo, s - e);
+    // FP32 forms, members with valid tile bounds: the exact pass over the
+    // tiles whose upper bound reaches L (the last stage raised screen_bits to
+    // the member's maximum lower bound), a warp per tile over every member's
+    // tiles in a fixed stride (k_dt_refine's tile pass)
+    auto tile_refine = [&]() {
+      const int lane = threadIdx.x & 31;
+      const int warps = int(gridDim.x) * (NT / 32);
+      const int total = __ldg(&b.work.tile_prefix[n]);
+      for (int t = int(blockIdx.x) * (NT / 32) + int(threadIdx.x >> 5); t < total; t += warps) {
+        const int m = WENOFD_IX(b.guard, owner(b.work.tile_prefix, n, t), n);
+        const BatchMember &M = b.members[m];
+        Ctrl *c = M.ctrl;
+        if (!__ldcg(&c->active) || !__ldcg(&c->bounds_valid)) continue;  // warp-uniform
+        const float L = __uint_as_float(__ldcg(&c->screen_bits));
+        const int local = t - __ldg(&b.work.tile_prefix[m]);
+        const int tiles_j = M.tiles_j;
+        // (bounds are allocated for tiles of 15 rows, the most tiles)
+        if (__ldcg(&M.tile_bounds[WENOFD_IX(b.guard, local, ((M.g.nx + 14) / 15) * tiles_j)]).y < L) continue;
+        const int i0 = (local / tiles_j) * TI, j = (local - (local / tiles_j) * tiles_j) * TJ + lane;
+        const int i1 = i0 + TI < M.g.nx ? i0 + TI : M.g.nx;
+        double smax = 0.0;
+        int nan_seen = 0;
+        SpeedMemo memo;
+        if (j < M.g.ny) {
+          for (int i = i0; i < i1; ++i) {
+            double rho, mu, mv, E;
+            node(M, (long long)i * M.g.ny + j, rho, mu, mv, E);
+            float s32, e;
+            screen_speed(M.g, rho, mu, mv, E, s32, e);
+            if (s32 + e >= L && !memo.repeat(rho, mu, mv, E)) {
+              const double sp = exact_speed(M.g, rho, mu, mv, E);
+              if (sp != sp) nan_seen = 1;
+              else if (sp > smax) smax = sp;
+            }
+          }
         }
-        for (int o = 16; o > 0; o >>= 1) lo = fmaxf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-        if ((threadIdx.x & 31) == 0) atomicMax(&M.ctrl->screen_bits, __float_as_uint(lo));
-      });
-      barrier(Nothing());
+        for (int o = 16; o > 0; o >>= 1) {
+          const double other = __shfl_xor_sync(0xffffffffu, smax, o);
+          smax = other > smax ? other : smax;
+          nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
+        }
+        if (lane == 0) {
+          atomicMax(&c->max_s_bits, (unsigned long long)__double_as_longlong(smax));
+          if (nan_seen) atomicOr(&c->nan_flag, 1);
+        }
+      }
+    };
+    // members without valid bounds: node chunks (FP64 form: every member)
+    auto chunk_pass = [&](int local, const BatchMember &M) {
+      if constexpr (F32)
+        if (__ldcg(&M.ctrl->bounds_valid)) return;  // block-uniform: the tile pass covers it
+      exact_pass(local, M);
+    };
+    if constexpr (F32) {
+      const bool all_valid = __ldcg(b.all_bounds) != 0;  // grid-uniform (set before the last release)
+      if (!all_valid) {
+        // screen of the members without valid bounds: L = max (s32 - e), a
+        // lower bound of the member's max s
+        for_member_items(b, cnt + 0, b.work.pt_prefix, sM, [&](int local, const BatchMember &M) {
+          if (__ldcg(&M.ctrl->bounds_valid)) return;  // block-uniform
+          const long long first = (long long)local * kPtChunk;
+          const long long npts = (long long)M.g.nx * M.g.ny;
+          float lo = 0.0f;
+          for (long long t = first + threadIdx.x; t < first + kPtChunk && t < npts; t += NT) {
+            double rho, mu, mv, E;
+            node(M, t, rho, mu, mv, E);
+            float s, e;
+            screen_speed(M.g, rho, mu, mv, E, s, e);
+            lo = fmaxf(lo, s - e);
+          }
+          for (int o = 16; o > 0; o >>= 1) lo = fmaxf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+          if ((threadIdx.x & 31) == 0) atomicMax(&M.ctrl->screen_bits, __float_as_uint(lo));
+        });
+        barrier(Nothing());
+        for_member_items(b, cnt + 1, b.work.pt_prefix, sM, chunk_pass);
+      }
+      tile_refine();
+    } else {
+      for_member_items(b, cnt + 1, b.work.pt_prefix, sM, exact_pass);
     }
-    for_member_items(b, cnt + 1, b.work.pt_prefix, sM, exact_pass);
     barrier(finalize);
 
     // m_now += dt; count++ (src/WENOFD.cpp:213-224), then the next step's
     // gate; after the launch's last step, the host summary
     const bool last_step = step == b.nsteps - 1;
+    // FP32 forms, SSP-RK2/3: the last stage screens the nodes it writes
+    constexpr bool kFused = F32;
+    const bool fused = kFused && b.rk != 0;
     auto step_end = [&]() {
-      int alive = 0, err = 0;
+      int alive = 0, err = 0, all = 1;
       for (int base = 0; base < n; base += NT) {
         const int m = base + int(threadIdx.x);
         int can = 0, e = 0;
@@ -262,6 +340,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
             c->now = now;
             c->steps = __ldcg(&c->steps) + 1;
             c->done = !(fabs(now - __ldcg(&c->t_end)) > 1e-9);
+            c->bounds_valid = fused ? 1 : 0;
           }
           can = runnable(c);
           c->active = can;
@@ -269,7 +348,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         }
         alive += __syncthreads_count(can);
         err |= __syncthreads_or(e);
+        all &= __syncthreads_and(!can || (m < n && __ldcg(&b.members[m].ctrl->bounds_valid)));
       }
+      if (F32 && threadIdx.x == 0) *b.all_bounds = all;
       if (last_step && threadIdx.x == 0) {
         b.status[0] = alive;
         b.status[1] = err;
@@ -310,8 +391,12 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? (NT <= 256 ? 3 : 1) : 1) 
         a.active = &M.ctrl->active;
         a.mode = kModeRK;
         a.flags = ROUTE ? M.flags : nullptr;
+        if (fused && st == nst - 1) {  // screen the new U^n into the member's tile bounds
+          a.bounds = M.tile_bounds;
+          a.screen = &M.ctrl->screen_bits;
+        }
         if constexpr (F32)
-          stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw);
+          stage_tile_f32<SCHEME, TI, TJ, NT, ROUTE, true, !(NT <= 256)>(M.g, a, ti * TI, tj * TJ, smem_raw, local);
         else stage_tile_f64<SCHEME, TI, TJ, NT, true>(M.g, a, ti * TI, tj * TJ, smem_raw);
       });
       if (st < nst - 1 || b.rk == 0) barrier(Nothing());

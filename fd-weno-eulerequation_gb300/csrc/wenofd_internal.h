@@ -147,6 +147,10 @@ struct BatchMember {
   const void *ind_weights;
   float ind_logit_threshold;
   int ind_bands;
+  // FP32 forms: the member's per-stage-tile time-step screen bounds (tiles
+  // of the batch's tile height), written by the last stage of a step; null
+  // for FP64 members.
+  float2 *tile_bounds;
 };
 
 // Exclusive prefix sums of work items per member (n+1 entries each).
@@ -180,6 +184,11 @@ struct BatchArgs {
   // its ghosts, as the single solve's indicator does.  Uses the counters of
   // step nsteps (the counter array then holds nsteps + 1 steps).
   int fill_end = 0;
+  // FP32 forms: set by the block that releases a barrier when every member
+  // that can step holds valid tile bounds of its U^n (Ctrl::bounds_valid):
+  // the next time-step reduction then skips its screen and node passes and
+  // refines only the candidate tiles.
+  int *all_bounds = nullptr;
   // Test instance only (k_batch with WITHHOLD): block `hold_block` skips its
   // arrival at the launch's barrier number `hold_barrier` (counted from 0).
   int hold_block = -1, hold_barrier = -1;
