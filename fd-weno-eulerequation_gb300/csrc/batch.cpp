@@ -207,6 +207,7 @@ int plan(wenofd_batch *b, int tile_i) {
     M.flags = b->learned ? s->flags : nullptr;
     M.ind_weights = ind ? s->ind_weights : nullptr;
     M.ind_logit_threshold = s->ind_logit_threshold;
+    M.ind_guard = s->ind_guard;
     M.ind_bands = int(ceil_div(ceil_div(s->nx, 4), wenofd::kIndBandTiles));
     M.tile_bounds = s->tile_bounds;
     b->ind_plan[m] = {M.ind_weights, M.ind_logit_threshold};

@@ -143,7 +143,8 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
   // The learned form classifies the nodes once per step, on the stage-1
   // input (ghosts just filled); all stages of the step route with those flags.
   if (s->precision == WENOFD_LEARNED && in == s->S && un == s->S && s->ind_ready) {
-    CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->flags, s->wait_error,
+    CUDA_TRY(wenofd::launch_indicator(s->g, in, s->ind_weights, s->ind_logit_threshold, s->ind_guard, s->flags,
+                                      s->wait_error,
                                       &s->ctrl->active, timeloop ? s->ctrl : nullptr, s->ind_interval,
                                       s->stream));
     s->launches += 1;
@@ -278,6 +279,9 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   int ind_interval = 1;
   if (!get_int(opt, "INDICATOR_INTERVAL", ind_interval, false) || ind_interval < 1 || ind_interval > 1000)
     return fail(WENOFD_BAD_CONFIG, "bad INDICATOR_INTERVAL");
+  double ind_guard = 0.0;
+  if (!get_double(opt, "INDICATOR_GUARD", ind_guard, false) || !(ind_guard >= 0.0) || ind_guard > 1e6)
+    return fail(WENOFD_BAD_CONFIG, "bad INDICATOR_GUARD");
   {
     auto it = opt.find("SEED");
     if (it != opt.end()) {
@@ -335,6 +339,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
   s->cfl = cfl;
   s->label_deviation = label_deviation;
   s->ind_interval = ind_interval;
+  s->ind_guard = float(ind_guard);
   s->cs = cs;
   const double dx = (cs.xr - cs.xl) / (nx - 1);  // src/WENOFD.cpp:73-74
   const double dy = (cs.yr - cs.yl) / (ny - 1);
@@ -832,7 +837,8 @@ int wenofd_indicator_flags(wenofd_solver *s, unsigned char *host_flags) {
   CUDA_TRY(cudaSetDevice(s->device));
   CUDA_TRY(wenofd::launch_ctrl_open(s->ctrl, s->stream));
   CUDA_TRY(wenofd::launch_bc_fill(s->g, s->S, s->special, nullptr, s->stream));
-  CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->flags, s->wait_error,
+  CUDA_TRY(wenofd::launch_indicator(s->g, s->S, s->ind_weights, s->ind_logit_threshold, s->ind_guard, s->flags,
+                                    s->wait_error,
                                     nullptr, nullptr, 1, s->stream));
   s->launches += 3;
   CUDA_TRY(cudaMemcpy2DAsync(host_flags, s->ny, s->flags + size_t(wenofd::kGhost) * s->g.pitch + wenofd::kGhost,

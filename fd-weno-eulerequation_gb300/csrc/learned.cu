@@ -345,9 +345,9 @@ __device__ __forceinline__ void gelu_row_store(const float z[32], __nv_bfloat16 
 // Normalised 5x5 window (normalise() in learned_common.cuh, same arithmetic)
 // written as BF16 into columns col0 .. col0+24 of row `row` of A1 in four
 // 16-byte chunks; columns col0+25 .. col0+31 take `tail` (two values, then
-// zeros).
-__device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A, int row, int col0, float tail0,
-                                             float tail1, unsigned long long *rec) {
+// zeros).  Returns the window's range R = max |v - v_centre|.
+__device__ __forceinline__ float window_store(const float w[25], __nv_bfloat16 *A, int row, int col0, float tail0,
+                                              float tail1, unsigned long long *rec) {
   constexpr int kc = kK1 / 8;
   const float c = w[12];
   // differences and scaling on packed FP32 pairs (two operations per
@@ -387,6 +387,7 @@ __device__ __forceinline__ void window_store(const float w[25], __nv_bfloat16 *A
     const int o = canon_off(row, col0 + 8 * ch, kc);
     *reinterpret_cast<uint4 *>(&A[WENOFD_SPAN(rec, o, o + 7, kCells * kK1)]) = q;
   }
+  return R;
 }
 
 constexpr int kResident = 8;  // CTAs per SM: 28 KB shared memory, 64 registers, 64 TMEM columns each
@@ -407,12 +408,14 @@ struct IndTc {
 
 // One band of indicator tiles: tiles first .. last-1 (4 rows x 32 columns of
 // cells each) down strip `strip` of the grid g, state U (ghosts filled),
-// flags written at flags[(kGhost + i) * flag_pitch + kGhost + j].  Every
+// flags written at flags[(kGhost + i) * flag_pitch + kGhost + j].  With
+// guard > 0 a cell is also flagged when the range of its density or pressure
+// window exceeds guard times the centre value (INDICATOR_GUARD).  Every
 // thread of the CTA calls it.  The node patch is a ring of 8 rows, node row
 // i in slot i & 7: consecutive tiles of a band share 4 of their 8 patch
 // rows, so every tile after the band's first loads 4 rows.  Returns false
 // when a tensor-core wait gave up (recorded in *error); the CTA then stops.
-__device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, float logit_threshold,
+__device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, float logit_threshold, float guard,
                                                unsigned char *flags, int flag_pitch, int *error, int strip, int first,
                                                int last, const IndSmem &sm, IndTc &tc) {
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -483,6 +486,7 @@ __device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, f
     }
     __syncthreads();
     // 2. features of cell (i0 + warp, j0 + lane) -> row tid of A1
+    bool guarded = false;
     {
       const int ci = warp, cj = tid & 31;
       int rows[5];  // ring slots of node rows i0 + ci - 2 .. i0 + ci + 2
@@ -493,12 +497,14 @@ __device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, f
       for (int a = 0; a < 5; ++a)
 #pragma unroll
         for (int b = 0; b < 5; ++b) w[a * 5 + b] = sRho[WENOFD_IX(g.guard, rows[a] + b, kPI * kPJ)];
-      window_store(w, sA1, tid, 0, 1.0f, 1.0f, g.guard);  // columns 25, 26: bias inputs
+      const float Rr = window_store(w, sA1, tid, 0, 1.0f, 1.0f, g.guard);  // columns 25, 26: bias inputs
+      guarded = guard > 0.0f && Rr > guard * fabsf(w[12]);
 #pragma unroll
       for (int a = 0; a < 5; ++a)
 #pragma unroll
         for (int b = 0; b < 5; ++b) w[a * 5 + b] = sPre[WENOFD_IX(g.guard, rows[a] + b, kPI * kPJ)];
-      window_store(w, sA1, tid, kColP, 0.0f, 0.0f, g.guard);
+      const float Rp = window_store(w, sA1, tid, kColP, 0.0f, 0.0f, g.guard);
+      guarded = guarded || (guard > 0.0f && Rp > guard * fabsf(w[12]));
     }
     // 3. layer 1 (bias included)
     if (!layer([&] { mma_layer<kK1, kHid>(tc.tmem, sA1, sm.B1); })) return false;
@@ -525,7 +531,7 @@ __device__ __forceinline__ bool indicator_band(const Geom &g, const double *U, f
       const int i = i0 + warp, j = j0 + (tid & 31);
       if (i < g.nx && j < g.ny && !tc.failed)
         flags[WENOFD_IX(g.guard, (long long)(kGhost + i) * flag_pitch + (kGhost + j), (long long)g.nxt * flag_pitch)] =
-            logit > logit_threshold ? 1 : 0;
+            (logit > logit_threshold || guarded) ? 1 : 0;
     }
     tc_fence_before();
     if (__syncthreads_or(tc.failed)) return false;
@@ -572,7 +578,7 @@ __device__ __forceinline__ void indicator_close(const IndTc &tc) {
 }
 
 __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, const double *U, const IndicatorWeights *W,
-                                                            float logit_threshold, unsigned char *flags,
+                                                            float logit_threshold, float guard, unsigned char *flags,
                                                             int flag_pitch, int *error, const int *active,
                                                             const Ctrl *ctrl, int interval) {
   if (active && *active == 0) return;
@@ -598,7 +604,7 @@ __global__ void __launch_bounds__(kCells, kResident) k_indicator_tc(Geom g, cons
   const int strip = int(blockIdx.x) % tiles_j, band = int(blockIdx.x) / tiles_j;
   const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
   const IndSmem sm{sA, sB1, sB2, sB3, sRho, sPre};
-  indicator_band(g, U, logit_threshold, flags, flag_pitch, error, strip, first, last, sm, tc);
+  indicator_band(g, U, logit_threshold, guard, flags, flag_pitch, error, strip, first, last, sm, tc);
   indicator_close(tc);
 }
 
@@ -663,7 +669,9 @@ __global__ void __launch_bounds__(kCells, kResident)
     const int local = item - __ldg(&prefix[m]);
     const int strip = local % tiles_j, band = local / tiles_j;
     const int first = int((long long)tiles_i * band / bands), last = int((long long)tiles_i * (band + 1) / bands);
-    if (!indicator_band(g, sM.S, sM.ind_logit_threshold, sM.flags, g.pitch, error, strip, first, last, sm, tc)) break;
+    if (!indicator_band(g, sM.S, sM.ind_logit_threshold, sM.ind_guard, sM.flags, g.pitch, error, strip, first, last,
+                        sm, tc))
+      break;
   }
   indicator_close(tc);
 }
@@ -719,7 +727,7 @@ void pack_indicator_weights(const float *params, void *host_out) {
   put(w->w3, 0, kHid + 1, kK2 / 8, lo);
 }
 
-cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
+cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold, float guard,
                              unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
                              cudaStream_t s) {
   const int tiles_i = (g.nx + lrn::kTileI - 1) / lrn::kTileI, tiles_j = (g.ny + lrn::kTileJ - 1) / lrn::kTileJ;
@@ -736,7 +744,7 @@ cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights
   bands = bands < 1 ? 1 : (bands > tiles_i ? tiles_i : bands);
   const int grid = tiles_j * bands;
   lrn::k_indicator_tc<<<grid, lrn::kCells, 0, s>>>(g, U, static_cast<const lrn::IndicatorWeights *>(weights),
-                                                   logit_threshold, flags, g.pitch, error, active, ctrl,
+                                                   logit_threshold, guard, flags, g.pitch, error, active, ctrl,
                                                    interval);
   return cudaGetLastError();
 }

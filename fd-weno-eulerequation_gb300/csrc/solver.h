@@ -34,6 +34,7 @@ struct wenofd_solver {
   float ind_logit_threshold = 0.0f;
   double label_deviation = 1e-2;  // LABEL_DEVIATION: training-label threshold
   int ind_interval = 1;            // INDICATOR_INTERVAL: steps per indicator run in the time loop
+  float ind_guard = 0.0f;          // INDICATOR_GUARD: relative window range that flags a node (0: off)
   bool ind_ready = false;
   cudaGraphExec_t graph = nullptr;   // graph_steps steps of the time loop
   cudaGraphExec_t graph1 = nullptr;  // one step, for the tail of a capped advance

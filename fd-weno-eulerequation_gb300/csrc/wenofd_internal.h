@@ -146,6 +146,7 @@ struct BatchMember {
   unsigned char *flags;
   const void *ind_weights;
   float ind_logit_threshold;
+  float ind_guard;  // INDICATOR_GUARD (0: off)
   int ind_bands;
   // FP32 forms: the member's per-stage-tile time-step screen bounds (tiles
   // of the batch's tile height), written by the last stage of a step; null
@@ -244,7 +245,9 @@ cudaError_t launch_sample_write(const Geom &g, const double *U, const unsigned c
 // With ctrl set (the time loop), the indicator runs only on steps whose
 // count since Ctrl::ind_base is a multiple of `interval`; the flags of the
 // last run route the steps in between.
-cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold,
+// guard > 0 (INDICATOR_GUARD): a node is also flagged when the range of its
+// 5x5 density or pressure window exceeds guard times the centre value.
+cudaError_t launch_indicator(const Geom &g, const double *U, const void *weights, float logit_threshold, float guard,
                              unsigned char *flags, int *error, const int *active, const Ctrl *ctrl, int interval,
                              cudaStream_t s);
 // Indicator runs of a learned batch: one launch over every member that can

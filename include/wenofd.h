@@ -78,7 +78,10 @@ const char *wenofd_version(void);
  * equation->outputtime), DEVICE, TILE_I (stage-kernel tile height; 0 =
  * default), LABEL_DEVIATION (training labels of wenofd_indicator_data;
  * default 1e-2), INDICATOR_INTERVAL (time steps per indicator run, see
- * wenofd_routing_flags; default 1), and overrides of the
+ * wenofd_routing_flags; default 1), INDICATOR_GUARD (learned form: a node
+ * is also flagged when the range of its 5x5 density or pressure window
+ * exceeds this fraction of the centre value, so strong jumps take WENO-Z
+ * whatever the network says; default 0 = off), and overrides of the
  * EulerEquation members the reference's callers may set on their equation
  * object (utils/equations.hpp:58-70): XL, XR, YL, YR, GAMMA, BC_LEFT,
  * BC_RIGHT, BC_BOTTOM, BC_TOP (BOUNDARYTYPE values), GRAVITY (0/1). */

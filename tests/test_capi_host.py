@@ -44,6 +44,10 @@ def test_version_string():
      "INDICATOR_INTERVAL"),
     ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "LABEL_DEVIATION": 0},
      "LABEL_DEVIATION"),
+    ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "INDICATOR_GUARD": -0.5},
+     "INDICATOR_GUARD"),
+    ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1, "INDICATOR_GUARD": "x"},
+     "INDICATOR_GUARD"),
     ({"TESTCASE": 0, "ELEMNUMX": 10, "ELEMNUMY": 10, "RKMETH": 2, "CFL": 0.5, "SCHEME": 1,
       "LABEL_DEVIATION": "x"}, "LABEL_DEVIATION"),
 ])

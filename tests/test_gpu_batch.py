@@ -157,6 +157,43 @@ def test_members_stop_at_their_own_end_time():
         assert np.array_equal(U, Ur)
 
 
+@pytest.mark.parametrize("precision", [wenofd.FP32, wenofd.LEARNED])
+def test_fp32_members_stop_at_their_own_end_time(precision):
+    """FP32 and learned members with different TEND: a member that has
+    finished no longer holds the others to the full time-step passes (the
+    reduction refines candidate tiles once every member that can step has
+    screened bounds), and every member ends at its own TEND with its single
+    solve's step count."""
+    tends = [0.004, 0.011, 0.002]
+    members = LEARNED_MEMBERS[:3] if precision == wenofd.LEARNED else MEMBERS[:3]
+    cfgs = [dict(_cfg(*m, precision, tend=t), INDICATOR_INTERVAL=2) for m, t in zip(members, tends)]
+    P = mlp_oracle.init_params(LEARNED_PARAMS_SEED)
+
+    def run(batched):
+        solvers = [wenofd.Solver(c) for c in cfgs]
+        try:
+            for s in solvers:
+                s.initialize()
+                if precision == wenofd.LEARNED:
+                    s.set_indicator(P, 0.5)
+            if batched:
+                with wenofd.Batch(solvers) as b:
+                    b.configure(steps_per_launch=3)
+                    b.advance(-1)
+            else:
+                for s in solvers:
+                    s.advance(max_steps=-1)
+            return [(s.get_state(), s.info().now, s.info().steps) for s in solvers]
+        finally:
+            for s in solvers:
+                s.close()
+
+    ref, got = run(False), run(True)
+    for (U, now, k), (Ur, nowr, kr), t in zip(got, ref, tends):
+        assert k == kr and abs(now - t) <= 1e-9
+        assert np.max(np.abs(U - Ur)) <= FP32_REL_TOL * np.max(np.abs(Ur))
+
+
 @pytest.mark.parametrize("precision", [wenofd.FP64, wenofd.FP32])
 def test_autotune_restores_state_and_keeps_results(precision):
     cfgs = [_cfg(*m, precision) for m in MEMBERS]

@@ -278,3 +278,73 @@ def test_indicator_interval_in_the_time_loop(interval):
         want = q.indicator_flags()
     assert np.array_equal(stored, want)
     assert 0.0 < want.mean() < 1.0
+
+
+def _window_range_ratio(G, gamma=1.4):
+    """max over each interior node's 5x5 window of |v - v_centre| / |v_centre|
+    for density and pressure (the larger of the two), from a ghosted state
+    [4][nx+8][ny+8] (float64; the kernel works on the state rounded to FP32)."""
+    rho = G[0]
+    p = (gamma - 1.0) * (G[3] - 0.5 * (G[1] ** 2 + G[2] ** 2) / rho)
+    nx, ny = G.shape[1] - 8, G.shape[2] - 8
+    out = np.zeros((nx, ny))
+    for v in (rho, p):
+        c = v[4:4 + nx, 4:4 + ny]
+        r = np.zeros((nx, ny))
+        for a in range(-2, 3):
+            for b in range(-2, 3):
+                r = np.maximum(r, np.abs(v[4 + a:4 + a + nx, 4 + b:4 + b + ny] - c))
+        out = np.maximum(out, r / np.abs(c))
+    return out
+
+
+def test_indicator_guard_flags_large_window_ranges():
+    """INDICATOR_GUARD = g: a node is flagged when its density or pressure
+    window's range exceeds g times the centre value, whatever the network
+    says.  With a network that flags nothing the flags are exactly that
+    condition (up to FP32 rounding of nodes within 0.1 % of the bound)."""
+    g = 0.5
+    p = _riemann_state(80, 64, 3, seed=6)
+    cfg = {"TESTCASE": 4, "ELEMNUMX": p.nx, "ELEMNUMY": p.ny, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1, "SEED": 6,
+           "PRECISION": wenofd.LEARNED, "INDICATOR_GUARD": g}
+    with wenofd.Solver(cfg) as s:
+        s.set_state(p.interior())
+        s.set_indicator(_constant_net(-50.0), 0.5)
+        flags = s.indicator_flags().astype(bool)
+        ratio = _window_range_ratio(s.get_state_ghosted())
+    with wenofd.Solver(dict(cfg, INDICATOR_GUARD=0.0)) as s:
+        s.set_state(p.interior())
+        s.set_indicator(_constant_net(-50.0), 0.5)
+        assert not s.indicator_flags().any()
+    assert 0 < flags.sum() < flags.size
+    assert np.all(flags[ratio > g * 1.001])
+    assert np.all(ratio[flags] >= g * 0.999)
+
+
+def test_indicator_guard_keeps_strong_jumps_physical():
+    """A network that misses shock faces sends them to the linear upwind
+    flux, which does not keep density and pressure positive at strong
+    jumps: with a seeded untrained network the four-quadrant Riemann problem
+    48x100 (seed 3) stops with NAN_DT within 30 steps.  With the guard at 0.5
+    every node whose window spans a jump of half its value takes WENO-Z, and
+    the same run completes, close to plain FP64 WENO-Z."""
+    P = mlp_oracle.init_params(7)
+    cfg = {"TESTCASE": 4, "ELEMNUMX": 48, "ELEMNUMY": 100, "RKMETH": 2, "CFL": 0.6, "SCHEME": 1, "SEED": 3,
+           "PRECISION": wenofd.LEARNED}
+    with wenofd.Solver(cfg) as s:
+        s.initialize()
+        s.set_indicator(P, 0.5)
+        with pytest.raises(wenofd.WenofdError) as e:
+            s.advance(max_steps=30)
+        assert e.value.status == wenofd.NAN_DT
+    with wenofd.Solver(dict(cfg, INDICATOR_GUARD=0.5)) as s:
+        s.initialize()
+        s.set_indicator(P, 0.5)
+        assert s.advance(max_steps=30) == 30
+        U = s.get_state()
+    with wenofd.Solver(dict(cfg, PRECISION=wenofd.FP64)) as s:
+        s.initialize()
+        assert s.advance(max_steps=30) == 30
+        U64 = s.get_state()
+    assert np.all(np.isfinite(U)) and np.all(U[0] > 0)
+    assert np.mean(np.abs(U[0] - U64[0])) <= 0.05 * np.mean(np.abs(U64[0]))
