@@ -511,6 +511,7 @@ int wenofd_get_info(const wenofd_solver *s, wenofd_info *info) {
   info->steps = s->ctrl_host->steps;
   info->launches = s->launches;
   info->graph_steps = s->graph_steps;
+  info->dt = s->ctrl_host->dt;
   return WENOFD_OK;
 }
 

@@ -1,6 +1,7 @@
 #include "WENOFD.hpp"
 
 #include <chrono>
+#include <numeric>
 #include <cmath>
 #include <ctime>
 #include <filesystem>
@@ -221,11 +222,23 @@ void CWENOFD::run(std::map<std::string, std::string> option) {
   outputAve("initial");
   std::cout << "Start iteration..." << std::endl;
   const auto t1 = std::chrono::steady_clock::now();
+  // The device time loop runs in chunks so that the reference's progress line
+  // (src/WENOFD.cpp:243-273: after steps 1, 21, 41, ...) can be printed: the
+  // first step alone, then chunks of a multiple of 20 steps that is also a
+  // multiple of the steps per graph replay (full replays only).
   long long steps = 0;
-  check(wenofd_advance(m_handle, -1, &steps), "run");
-  const auto t2 = std::chrono::steady_clock::now();
   wenofd_info info;
-  check(wenofd_get_info(m_handle, &info), "wenofd_get_info");
+  for (long long chunk = 1;;) {
+    long long k = 0;
+    check(wenofd_advance(m_handle, chunk, &k), "run");
+    steps += k;
+    check(wenofd_get_info(m_handle, &info), "wenofd_get_info");
+    if (k > 0 && steps % 20 == 1) progressLine(steps, info.dt, info.now, t1);
+    if (k < chunk) break;
+    const long long K = info.graph_steps > 0 ? info.graph_steps : 1;
+    chunk = std::lcm(20LL, K);
+  }
+  const auto t2 = std::chrono::steady_clock::now();
   m_now = info.now;
   m_steps = info.steps;
   downloadState();
@@ -238,6 +251,25 @@ void CWENOFD::run(std::map<std::string, std::string> option) {
   std::cout << "steps " << steps << ", t = " << m_now << ", loop " << loop_s << " s, "
             << double(m_worldPointNumX) * m_worldPointNumY * steps / loop_s << " cell-updates/s, total "
             << std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() << " s" << std::endl;
+}
+
+// The progress line of src/WENOFD.cpp:247-272 (iteration count, deltaT,
+// elapsed time, progress with a 50-character bar).
+void CWENOFD::progressLine(long long count, double deltaT, double now,
+                           std::chrono::steady_clock::time_point start) const {
+  const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - start).count();
+  const double progress = now / m_outputTime;
+  const int barWidth = 50;
+  const int pos = static_cast<int>(progress * barWidth);
+  std::cout << std::fixed << std::setprecision(2) << "Iteration count: " << count << std::scientific
+            << std::setprecision(2) << ", DeltaT: " << deltaT << std::fixed << std::setprecision(2)
+            << ", Elapsed time: " << elapsed << " seconds"
+            << ", Progress: " << now << "/" << m_outputTime << " (" << (progress * 100.0) << "%)"
+            << " [";
+  for (int i = 0; i < barWidth; ++i) std::cout << (i < pos ? "=" : (i == pos ? ">" : " "));
+  std::cout << "]" << std::endl;
+  std::cout.unsetf(std::ios::floatfield);
+  std::cout << std::setprecision(6);
 }
 
 // outputAve, src/WENOFD.cpp:1161-1238: Tecplot ASCII, point data packing.

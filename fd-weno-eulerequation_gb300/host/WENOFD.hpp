@@ -16,6 +16,7 @@
 //    it (backupProjectFiles).
 #pragma once
 
+#include <chrono>
 #include <map>
 #include <string>
 #include <vector>
@@ -87,6 +88,7 @@ class CWENOFD {
  private:
   void ensureHandle();
   void stepWith(RKMETHOD m, double dt);
+  void progressLine(long long count, double deltaT, double now, std::chrono::steady_clock::time_point start) const;
   std::map<std::string, std::string> m_option;
   wenofd_solver *m_handle = nullptr;
 };

@@ -48,6 +48,7 @@ class Info(C.Structure):
         ("steps", C.c_longlong),
         ("launches", C.c_longlong),
         ("graph_steps", C.c_int),
+        ("dt", C.c_double),
     ]
 
 

@@ -64,6 +64,7 @@ typedef struct wenofd_info {
   long long steps;        /* completed time steps */
   long long launches;     /* kernels this handle has enqueued (graph nodes counted per replay) */
   int graph_steps;        /* time steps per CUDA-graph replay in wenofd_advance (0: not built yet) */
+  double dt;              /* the last time step (calculateDeltaT's deltaT); 0 before the first */
 } wenofd_info;
 
 /* Message describing the last failure on the calling thread ("" if none). */

@@ -51,4 +51,10 @@ def test_driver_reproduces_reference_output_files(tmp_path):
     a = np.array([float(x) for x in ours[1].split(",")])
     b = np.array([float(x) for x in ref[1].split(",")])
     assert np.allclose(a, b, rtol=1e-9, atol=0)
+    # the reference's progress line (src/WENOFD.cpp:247-272) after step 1 and
+    # after every device chunk (a multiple of 20 steps), so at counts 1 mod 20
+    prog = [ln for ln in r.stdout.splitlines() if ln.startswith("Iteration count: ")]
+    counts = [int(ln.split(",")[0].split(": ")[1]) for ln in prog]
+    assert counts and counts[0] == 1 and all(c % 20 == 1 for c in counts) and counts == sorted(counts)
+    assert all(", DeltaT: " in ln and " seconds, Progress: " in ln and ln.endswith("]") for ln in prog)
     shutil.rmtree(tmp_path / "output")
