@@ -44,7 +44,8 @@ def test_readme_convergence_table(scheme):
 
 
 def test_fifth_order_at_t2():
-    """The BASELINE C1 end time t = 2 (the reference hard-codes t = 1)."""
+    """The smooth wave's convergence to the end time t = 2 (the reference
+    hard-codes t = 1, utils/equations.hpp:412)."""
     l1 = [_norms(n, wenofd.WENOJS, t_end=2.0)[1] for n in (100, 140, 200)]
     order = np.log(l1[0] / l1[2]) / np.log(2.0)
     assert order > 4.7, (l1, order)
