@@ -270,14 +270,16 @@ __device__ __forceinline__ void stage_tile_f32(const Geom &g, const StageArgs &a
   const float gamma = g.gamma32, zpl = g.zpl32;
   const bool stage1 = a.form == kFormStage1;
 
-  // Stages 2 and 3 without KEEP read U^n only in the epilogue, the first
-  // touch of those lines in this launch: ask L2 for them now, so that the
-  // epilogue's loads hit L2 instead of waiting on DRAM.  A tile row of 32
-  // doubles from ghosted column j0 + 4 (rows start on 256-byte boundaries,
-  // j0 a multiple of 32) spans three 128-byte lines, holding the tile's
-  // columns -4..11, 12..27 and 28..43: one prefetch at columns 0, 12 and 28
-  // (clamped to the grid) per row and component.
-  if constexpr (!COH && !KEEP) {
+  // Stages 2 and 3 that do not stage U^n by cp.async (without KEEP, or in
+  // the persistent batched kernel) read it only in the epilogue, the first
+  // touch of those lines in this tile: ask L2 for them now, so that the
+  // epilogue's loads hit L2 instead of waiting on DRAM (a hint only; L2 is
+  // where the batched kernel's loads see other blocks' writes anyway).  A
+  // tile row of 32 doubles from ghosted column j0 + 4 (rows start on
+  // 256-byte boundaries, j0 a multiple of 32) spans three 128-byte lines,
+  // holding the tile's columns -4..11, 12..27 and 28..43: one prefetch at
+  // columns 0, 12 and 28 (clamped to the grid) per row and component.
+  if constexpr (COH || !KEEP) {
     if (a.mode == kModeRK && !stage1) {
       constexpr int kLines = 3;
       for (int t = threadIdx.x; t < 4 * TI * kLines; t += NT) {
