@@ -149,11 +149,11 @@ int launch_stage(wenofd_solver *s, const double *in, const double *un, double *o
                                       s->stream));
     s->launches += 1;
   }
+  args.wait_error = s->wait_error;
   if (s->precision != WENOFD_FP64) {
-    args.wait_error = s->wait_error;
     CUDA_TRY(wenofd::launch_stage_fp32(s->g, args, s->tma[stage_buffer(s, in)], s->scheme, s->tile_i, s->stream));
   } else {
-    CUDA_TRY(wenofd::launch_stage_fp64(s->g, args, s->scheme, s->tile_i, s->stream));
+    CUDA_TRY(wenofd::launch_stage_fp64(s->g, args, s->tma[stage_buffer(s, in)], s->scheme, s->tile_i, s->stream));
   }
   return WENOFD_OK;
 }
@@ -372,7 +372,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
     const size_t tiles = size_t((nx + 14) / 15) * size_t((ny + 31) / 32);
     ok = cudaMalloc(&s->tile_bounds, tiles * sizeof(float2)) == cudaSuccess;
   }
-  if (ok && precision != WENOFD_FP64)
+  if (ok)  // the stage tiles' TMA waits (and the indicator's) report here
     ok = cudaMalloc(&s->wait_error, sizeof(int)) == cudaSuccess &&
          cudaMemsetAsync(s->wait_error, 0, sizeof(int), s->stream) == cudaSuccess;
   if (ok && precision == WENOFD_LEARNED) {
@@ -385,7 +385,7 @@ int create_from_map(const std::map<std::string, std::string> &opt, wenofd_solver
     cudaGetLastError();
     return bail(fail(WENOFD_CUDA_ERROR, "device allocation failed"));
   }
-  if (precision != WENOFD_FP64) {  // TMA maps of the three stage inputs
+  {  // TMA maps of the three stage inputs
     double *bufs[3] = {s->S, s->A, s->B};
     for (int k = 0; k < 3; ++k)
       if ((e = wenofd::make_stage_tma(s->g, bufs[k], s->flags, tile_i, &s->tma[k])) != cudaSuccess)
@@ -788,7 +788,8 @@ int wenofd_time_stages(wenofd_solver *s, int reps, double *ms_per_launch) {
       cudaError_t e = s->precision != WENOFD_FP64
                           ? wenofd::launch_stage_fp32(s->g, a, s->tma[stage_buffer(s, x.in)], s->scheme, s->tile_i,
                                                       s->stream)
-                          : wenofd::launch_stage_fp64(s->g, a, s->scheme, s->tile_i, s->stream);
+                          : wenofd::launch_stage_fp64(s->g, a, s->tma[stage_buffer(s, x.in)], s->scheme, s->tile_i,
+                                                      s->stream);
       CUDA_TRY(e);
       s->launches += 1;
     }

@@ -54,7 +54,7 @@ cudaError_t make_stage_tma(const Geom &g, const double *state, const unsigned ch
                            StageTma *out) {
   PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   if (!encode || !out || !state) return cudaErrorInvalidValue;
-  const int ti = tile_i == 31 ? 31 : 15;
+  const int ti = (tile_i == 31 || tile_i == 7) ? tile_i : 15;
   *out = StageTma{};
   {
     using S = dev::StageSmem32<15, 32>;

@@ -6,12 +6,14 @@
 
 namespace wenofd {
 
-cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s) {
-  const StageTma none{};  // the FP64 tile loads its halo per thread
+// The tile's halo arrives by TMA through the map in `tma` (make_stage_tma
+// for this tile height).
+cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, const StageTma &tma, int scheme, int tile_i,
+                              cudaStream_t s) {
   switch (tile_i) {
     case 0:
-    case 15: return dev::launch_stage_tile<double, 15, 256>(g, a, none, scheme, s);
-    case 7: return dev::launch_stage_tile<double, 7, 256>(g, a, none, scheme, s);
+    case 15: return dev::launch_stage_tile<double, 15, 256>(g, a, tma, scheme, s);
+    case 7: return dev::launch_stage_tile<double, 7, 256>(g, a, tma, scheme, s);
   }
   return cudaErrorInvalidValue;
 }

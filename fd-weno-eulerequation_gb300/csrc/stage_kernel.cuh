@@ -29,13 +29,24 @@ namespace wenofd {
 namespace dev {
 
 // Shared memory of the FP64 tile, structure of arrays [component][row][col].
+// The state tile's rows are kBoxJ = 40 doubles wide, halo node hj at column
+// hj + 1: the TMA box of the per-solve kernel (40 columns from the even,
+// 16-byte aligned column before the halo, TI + 6 rows, 4 planes) lands in
+// place, with no copy; the batched kernel's per-thread loads use the same
+// layout.
 template <int TI, int TJ>
 struct StageSmem {
   static constexpr int HI = TI + 6, HJ = TJ + 6;
-  static constexpr int kU = 4 * HI * HJ;                                    // state + halo
+  static constexpr int kBoxJ = 40;
+  static_assert(HJ + 2 <= kBoxJ, "box width");
+  static constexpr int kU = 4 * HI * kBoxJ;                                 // state + halo
+  static constexpr unsigned kBoxBytes = unsigned(kU) * 8u;
   static constexpr int kSplit = 4 * (HI * TJ > TI * HJ ? HI * TJ : TI * HJ);  // one of F+, F-
   static constexpr int kFace = 4 * ((TI + 1) * TJ > TI * (TJ + 1) ? (TI + 1) * TJ : TI * (TJ + 1));
-  static constexpr size_t bytes = sizeof(double) * (size_t(kU) + 2 * kSplit + kFace);
+  // 128 bytes of slack: the base is rounded up to 128 bytes (TMA destination)
+  static constexpr size_t bytes = 128 + sizeof(double) * (size_t(kU) + 2 * kSplit + kFace);
+  // index of state component r at halo node (hi, hj)
+  static __device__ __forceinline__ int u(int r, int hi, int hj) { return (r * HI + hi) * kBoxJ + hj + 1; }
 };
 
 // One FP64 tile (TI x TJ interior nodes starting at i0, j0) of one RK stage,
@@ -45,23 +56,51 @@ struct StageSmem {
 // the persistent batched kernel.  COH: the tile's inputs may have been
 // written earlier in the same kernel by other blocks (the persistent batched
 // kernel): loads then go through L2 only (ld.global.cg) instead of the
-// non-coherent read-only path.
-template <int SCHEME, int TI, int TJ, int NT, bool COH = false>
+// non-coherent read-only path.  TMA (the per-solve kernel): the halo box
+// arrives by TMA through the map in `tma` (one thread issues it; a bounded
+// wait, on give-up the block records the error in a.wait_error and leaves
+// the tile); otherwise every thread loads nodes.
+template <int SCHEME, int TI, int TJ, int NT, bool COH = false, bool TMA = false>
 __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a, const int i0, const int j0,
-                                               unsigned char *smem_raw) {
+                                               unsigned char *smem_raw, const StageTma *tma = nullptr) {
   using T = double;
   using S = StageSmem<TI, TJ>;
   constexpr int HI = S::HI, HJ = S::HJ;
-  T *Us = reinterpret_cast<T *>(smem_raw);
+  unsigned char *base = smem_raw + (((tma_smem_addr(smem_raw) + 127u) & ~127u) - tma_smem_addr(smem_raw));
+  T *Us = reinterpret_cast<T *>(base);
   T *Fp = Us + S::kU;
   T *Fm = Fp + S::kSplit;
   T *Hf = Fm + S::kSplit;
   const T gamma = g.gamma, zpl = g.zp_lambda;
 
-  // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj.  All of a
-  // thread's loads are issued before any is used, so they are in flight
-  // together.
-  {
+  // --- state tile with halo: nodes ei = 4+i0-3+hi, ej = 4+j0-3+hj.
+  if constexpr (TMA) {
+    // box column c = ghosted column j0 + c = halo node hj = c - 1; box row 0 =
+    // ghosted row 1 + i0 (rows or columns past the array read as zero, like
+    // the per-thread loads, and feed only faces that are not computed)
+    __shared__ __align__(8) unsigned long long tma_bar;
+    if (threadIdx.x == 0) tma_bar_init(tma_smem_addr(&tma_bar), 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const unsigned bar = tma_smem_addr(&tma_bar);
+      tma_fence_proxy();
+      tma_bar_expect(bar, S::kBoxBytes);
+      // first coordinate x * 8 bytes a multiple of 16 (j0 is a multiple of
+      // 32; an unissued copy leaves the wait below to give up)
+      if (WENOFD_REQUIRE(g.guard, (j0 & 1) == 0, j0, 2)) tma_load_3d(tma_smem_addr(Us), &tma->u, j0, 1 + i0, 0, bar);
+    }
+    const bool ok = tma_bar_wait(tma_smem_addr(&tma_bar), 0, kTmaWaitLimit);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        if (a.wait_error) atomicExch(a.wait_error, 1);
+        tma_bar_wait(tma_smem_addr(&tma_bar), 0, kTmaWaitLimit);
+      }
+      __syncthreads();
+      return;
+    }
+  } else {
+    // All of a thread's loads are issued before any is used, so they are in
+    // flight together.
     constexpr int NLD = (4 * HI * HJ + NT - 1) / NT;
     double v[NLD];
 #pragma unroll
@@ -78,7 +117,12 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
 #pragma unroll
     for (int k = 0; k < NLD; ++k) {
       const int t = threadIdx.x + k * NT;
-      if (t < 4 * HI * HJ) Us[WENOFD_IX(g.guard, t, S::kU)] = v[k];
+      if (t < 4 * HI * HJ) {
+        const int r = t / (HI * HJ);
+        const int rem = t - r * (HI * HJ);
+        const int hi = rem / HJ, hj = rem - hi * HJ;
+        Us[WENOFD_IX(g.guard, S::u(r, hi, hj), S::kU)] = v[k];
+      }
     }
   }
   __syncthreads();
@@ -88,7 +132,7 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     const int hi = t / TJ, j = t - hi * TJ;
     T q[4], fm[4], fp[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, (r * HI + hi) * HJ + j + 3, S::kU)];
+    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, S::u(r, hi, j + 3), S::kU)];
     flux_split<T, 0>(gamma, q, fm, fp);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -104,8 +148,8 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     T um[4], u0[4], out[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      um[r] = Us[WENOFD_IX(g.guard, (r * HI + f + 2) * HJ + j + 3, S::kU)];
-      u0[r] = Us[WENOFD_IX(g.guard, (r * HI + f + 3) * HJ + j + 3, S::kU)];
+      um[r] = Us[WENOFD_IX(g.guard, S::u(r, f + 2, j + 3), S::kU)];
+      u0[r] = Us[WENOFD_IX(g.guard, S::u(r, f + 3, j + 3), S::kU)];
     }
     // stencils: nodes 0..4 TJ apart, components HI TJ apart
     face_flux<T, 0, SCHEME>(gamma, zpl, um, u0,
@@ -141,7 +185,7 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     const int i = t / HJ, hj = t - i * HJ;
     T q[4], fm[4], fp[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + hj, S::kU)];
+    for (int r = 0; r < 4; ++r) q[r] = Us[WENOFD_IX(g.guard, S::u(r, i + 3, hj), S::kU)];
     flux_split<T, 1>(gamma, q, fm, fp);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -156,8 +200,8 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     T um[4], u0[4], out[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      um[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + f + 2, S::kU)];
-      u0[r] = Us[WENOFD_IX(g.guard, (r * HI + i + 3) * HJ + f + 3, S::kU)];
+      um[r] = Us[WENOFD_IX(g.guard, S::u(r, i + 3, f + 2), S::kU)];
+      u0[r] = Us[WENOFD_IX(g.guard, S::u(r, i + 3, f + 3), S::kU)];
     }
     // stencils: nodes 0..4 adjacent, components TI HJ apart
     face_flux<T, 1, SCHEME>(gamma, zpl, um, u0,
@@ -187,8 +231,8 @@ __device__ __forceinline__ void stage_tile_f64(const Geom &g, const StageArgs &a
     const long long gidx = WENOFD_NODE(g, i0 + i, j0 + j);
     if (g.gravity) {  // RTI, g = 1 (src/WENOFD.cpp:807-813)
       const T g_g0 = T(1.0);
-      rr[3] += Us[WENOFD_IX(g.guard, (2 * HI + i + 3) * HJ + j + 3, S::kU)] * g_g0;
-      rr[2] += Us[WENOFD_IX(g.guard, (0 * HI + i + 3) * HJ + j + 3, S::kU)] * g_g0;
+      rr[3] += Us[WENOFD_IX(g.guard, S::u(2, i + 3, j + 3), S::kU)] * g_g0;
+      rr[2] += Us[WENOFD_IX(g.guard, S::u(0, i + 3, j + 3), S::kU)] * g_g0;
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -232,7 +276,8 @@ __global__ void __launch_bounds__(NT, stage_blocks_per_sm<T, ROUTE, NT>())
         g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw, int(blockIdx.y * gridDim.x + blockIdx.x),
         &tma);
   else
-    stage_tile_f64<SCHEME, TI, TJ, NT>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw);
+    stage_tile_f64<SCHEME, TI, TJ, NT, false, true>(g, a, int(blockIdx.y) * TI, int(blockIdx.x) * TJ, smem_raw,
+                                                    &tma);
 }
 
 // Dynamic shared memory of one stage tile.

@@ -96,7 +96,7 @@ struct StageTma {
   CUtensorMap flags;
 };
 // Encodes the maps of one state array (and of the flag array, if not null)
-// for stage tiles of tile_i rows (15 or 31).
+// for stage tiles of tile_i rows (FP32 tiles 15 or 31, FP64 tiles 15 or 7).
 cudaError_t make_stage_tma(const Geom &g, const double *state, const unsigned char *flags, int tile_i,
                            StageTma *out);
 enum { kModeRK = 0, kModeRHS = 1 };
@@ -122,8 +122,10 @@ unsigned long long *guard_record();
 cudaError_t launch_guard_selftest(unsigned long long *rec, int *buf, unsigned long long *site, cudaStream_t s);
 
 // stage kernels (stage_fp64.cu: parity arithmetic; stage_fp32.cu: FP32 form,
-// routed by a.flags when it is set)
-cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, int scheme, int tile_i, cudaStream_t s);
+// routed by a.flags when it is set); both take their halo by TMA through the
+// maps in `tma` (make_stage_tma for the same tile height)
+cudaError_t launch_stage_fp64(const Geom &g, const StageArgs &a, const StageTma &tma, int scheme, int tile_i,
+                              cudaStream_t s);
 // The FP32 tiles load their halo by TMA: `tma` holds the maps of a.uin (and
 // of a.flags) for tiles of tile_i rows.
 cudaError_t launch_stage_fp32(const Geom &g, const StageArgs &a, const StageTma &tma, int scheme, int tile_i,

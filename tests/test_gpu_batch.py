@@ -331,13 +331,15 @@ LEARNED_MEMBERS = [
 LEARNED_PARAMS_SEED = 7
 
 
-def _learned_run(interval, steps, batched, rk=2, configure=None, autotune=0, weights=(True,) * 5, late=0):
+def _learned_run(interval, steps, batched, rk=2, configure=None, autotune=0, weights=(True,) * 5, late=0,
+                 guard=0.0, members=None):
     """States, times, step counts and routing flags of the learned members
     after `late` steps without indicator weights (every face WENO), then
     loading the weights of the members marked in `weights`, then `steps`
     steps: in one batch, or each member alone (wenofd_advance)."""
     P = mlp_oracle.init_params(LEARNED_PARAMS_SEED)
-    cfgs = [dict(_cfg(*m, wenofd.LEARNED), RKMETH=rk, INDICATOR_INTERVAL=interval) for m in LEARNED_MEMBERS]
+    cfgs = [dict(_cfg(*m, wenofd.LEARNED), RKMETH=rk, INDICATOR_INTERVAL=interval, INDICATOR_GUARD=guard)
+            for m in (members or LEARNED_MEMBERS)]
     solvers = [wenofd.Solver(c) for c in cfgs]
     try:
         for s in solvers:
@@ -411,3 +413,13 @@ def test_learned_batch_without_weights_and_weights_loaded_later():
     for (_, _, _, fl), w in zip(got, weights):
         if not w:
             assert np.all(fl == 1)
+
+
+def test_learned_batch_with_guard_matches_single_solves():
+    """INDICATOR_GUARD reaches the batched indicator: guarded members,
+    including the seeded Riemann problem that stops with NAN_DT unguarded
+    (48x100, seed 3), run their steps with the single solves' flags."""
+    members = LEARNED_MEMBERS[:3] + [(orc.RIEMANN_SEEDED, 48, 100, 3, {})]
+    ref = _learned_run(2, 12, False, weights=(True,) * 4, guard=0.5, members=members)
+    got = _learned_run(2, 12, True, weights=(True,) * 4, guard=0.5, members=members)
+    _assert_learned_close(got, ref)
