@@ -338,27 +338,37 @@ def train_indicator(torch, device: int):
 def finer_reference_errors(wenofd, params, device: int, n: int = 1025, t_end: float = 0.1) -> dict:
     """L1 density error of each form against plain FP64 WENO-Z on the 2x
     finer node grid (2n-1)^2 at the same end time (fine node 2k = coarse node
-    k): the shear layer (seed SEED) at n^2, and a seeded four-quadrant Riemann
+    k): the shear layer (seed SEED) at n^2, the fine grid starting from the
+    coarse initial state refined (wenofd.refine: the same perturbation, not
+    the fine grid's own seeded noise), and a seeded four-quadrant Riemann
     problem (seed 31) at 257^2."""
     import numpy as np
 
-    def state_at(m, prec, par=None, riemann=False):
+    from wenofd.refine import shear_layer_refined
+
+    def state_at(m, prec, par=None, riemann=False, init=None, initial=False):
         cfg = dict(config_for(prec, device), ELEMNUMX=m, ELEMNUMY=m, TEND=t_end)
         if riemann:
             cfg.update(TESTCASE=4, SEED=31)
         with wenofd.Solver(cfg) as s:
-            s.initialize()
+            if init is None:
+                s.initialize()
+            else:
+                s.set_state(init)
+            if initial:
+                return s.get_state()
             if par is not None:
                 s.set_indicator(par, THRESHOLD)
             s.advance(-1)
             return s.get_state()[0]
 
-    fine = state_at(2 * n - 1, wenofd.FP64)[::2, ::2]
+    fine = state_at(2 * n - 1, wenofd.FP64, init=shear_layer_refined(state_at(n, wenofd.FP64, initial=True)))[::2, ::2]
     e = {name: float(np.mean(np.abs(state_at(n, prec, par) - fine)))
          for name, prec, par in (("fp64", wenofd.FP64, None), ("fp32", wenofd.FP32, None),
                                  ("learned_fp32", wenofd.LEARNED, params))}
     e["ratio_learned_to_fp64"] = e["learned_fp32"] / e["fp64"]
-    e["setup"] = f"shear layer {n}^2 vs {2 * n - 1}^2 plain FP64 WENO-Z, t = {t_end}"
+    e["setup"] = (f"shear layer {n}^2 vs {2 * n - 1}^2 plain FP64 WENO-Z from the refined coarse initial state, "
+                  f"t = {t_end}")
     m = 257
     fine = state_at(2 * m - 1, wenofd.FP64, riemann=True)[::2, ::2]
     r = {name: float(np.mean(np.abs(state_at(m, prec, par, riemann=True) - fine)))
@@ -524,6 +534,8 @@ def main() -> None:
                     help="WENO-Z weight deviation that labels a training node")
     ap.add_argument("--indicator-interval", type=int, default=INDICATOR_INTERVAL,
                     help="time steps per indicator run in the time loop")
+    ap.add_argument("--only-accuracy", type=int, default=0, metavar="N",
+                    help="only the accuracy leg, with the shear layer at N^2 against the (2N-1)^2 FP64 solution")
     ap.add_argument("--only-batching", action="store_true",
                     help="run the batching leg only (FP32, learned and FP64 batches vs one at a time): for profiling")
     ap.add_argument("--only-fp32", action="store_true",
@@ -584,6 +596,14 @@ def main() -> None:
             print(json.dumps({"fp32_form": {"value": args.steps * cells / (ms32 / 1e3), "unit": "cell-updates/s",
                                             "ms_per_step": ms32 / args.steps, "gpu_launches": launches},
                               "note": "FP32 form only (profiling run)"}))
+        return
+    if args.only_accuracy:
+        params, _ = train_indicator(torch, local)
+        t0 = time.perf_counter()
+        err = finer_reference_errors(wenofd, params, local, n=args.only_accuracy)
+        if rank == 0:
+            print(json.dumps({"vs_2x_finer_fp64": err, "seconds": round(time.perf_counter() - t0, 1),
+                              "note": "accuracy leg only"}))
         return
     if args.only_batching:
         params, _ = train_indicator(torch, local)

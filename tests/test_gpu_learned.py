@@ -200,23 +200,31 @@ def test_learned_error_on_the_shear_layer_at_1025():
     trains: two shear layers and two Riemann problems at other seeds, labels
     at WENO-Z weight deviation 1e-2, seed 7; threshold 0.8, indicator every
     fourth step) against a plain FP64 WENO-Z solution on the 2x finer 2049^2
-    grid (fine node 2k = coarse node k); its L1 density error is at most 1.5x
-    that of plain FP64 at 1025^2."""
+    grid (fine node 2k = coarse node k) started from the coarse initial state
+    refined (wenofd.refine: the same perturbation); its L1 density error is
+    at most 1.5x that of plain FP64 at 1025^2."""
+    from wenofd.refine import shear_layer_refined
+
     X, y = learned.generate_dataset(torch, label_deviation=1e-2)
     params, _ = learned.train(torch, X, y, epochs=30, batch=4096, lr=3e-3, seed=7)
     del X, y
 
-    def state_at(n, prec, par=None):
+    def state_at(n, prec, par=None, init=None, initial=False):
         with wenofd.Solver({"TESTCASE": 5, "ELEMNUMX": n, "ELEMNUMY": n, "RKMETH": 2, "CFL": 0.7, "SCHEME": 1,
                             "SEED": 2024, "PRECISION": prec, "TEND": 0.1, "INDICATOR_INTERVAL": 4}) as s:
-            s.initialize()
+            if init is None:
+                s.initialize()
+            else:
+                s.set_state(init)
+            if initial:
+                return s.get_state()
             if par is not None:
                 s.set_indicator(par, 0.8)
             s.advance(-1)
             return s.get_state()[0]
 
     n = 1025
-    fine = state_at(2 * n - 1, wenofd.FP64)[::2, ::2]
+    fine = state_at(2 * n - 1, wenofd.FP64, init=shear_layer_refined(state_at(n, wenofd.FP64, initial=True)))[::2, ::2]
     e64 = float(np.mean(np.abs(state_at(n, wenofd.FP64) - fine)))
     e32 = float(np.mean(np.abs(state_at(n, wenofd.FP32) - fine)))
     elr = float(np.mean(np.abs(state_at(n, wenofd.LEARNED, params) - fine)))
